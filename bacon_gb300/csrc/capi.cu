@@ -1,0 +1,673 @@
+// C ABI of the engine: contexts, the builder mirror, validation, and the
+// host side of the batched solves (staging, launch configuration, CUDA-graph
+// cache).  See include/bacon_gb300.h for the reference interfaces replaced.
+#include "bacon_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "plain.h"
+#include "registry.h"
+#include "rk_kernel.cuh"
+
+namespace bacon {
+double measure_fp64_fma_gflops(cudaStream_t stream, int num_sms);
+}
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define BACON_CUDA(expr)                                                                     \
+  do {                                                                                       \
+    cudaError_t e_ = (expr);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(BACON_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+// Grow-only device allocation owned by a context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+uint64_t fnv1a(const void* data, size_t len, uint64_t h = 1469598103934665603ull) {
+  const unsigned char* b = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < len; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+int expected_dim(int rhs) {
+  switch (rhs) {
+    case BACON_RHS_HARMONIC:
+    case BACON_RHS_VDP:
+    case BACON_RHS_LOTKA:
+      return 2;
+    case BACON_RHS_LORENZ:
+    case BACON_RHS_ROBERTSON:
+      return 3;
+    default:
+      return -1;  // any
+  }
+}
+
+int expected_params(int rhs, int dim) {
+  switch (rhs) {
+    case BACON_RHS_VDP: return 1;
+    case BACON_RHS_LORENZ: return 3;
+    case BACON_RHS_LOTKA: return 4;
+    case BACON_RHS_ROBERTSON: return 3;
+    case BACON_RHS_CHAIN: return dim / 2 + 1;
+    default: return 0;
+  }
+}
+
+}  // namespace
+
+struct bacon_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  unsigned long long* d_ctl = nullptr;  // [0] work counter [1] first failing index [2] live
+  unsigned long long* h_ctl = nullptr;  // pinned mirror
+  std::vector<bacon::RkEntry> kernels;
+  DevBuf in_y0, in_params, in_t0, in_tend, out_y, out_t, out_acc, out_rej, out_st, out_tt, out_ty;
+  DevBuf pl_y, pl_K, pl_t, pl_dt, pl_end, pl_att, pl_acc, pl_rej, pl_st;
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::unordered_map<uint64_t, Graph> graphs;
+  std::unordered_map<uint64_t, std::pair<int, int>> tuned;
+  int64_t launches = 0;
+};
+
+extern "C" {
+
+const char* bacon_last_error(void) { return g_last_error.c_str(); }
+
+int bacon_ctx_create(int device, bacon_ctx** out) {
+  if (!out) return fail(BACON_INVALID_ARGUMENT, "bacon_ctx_create: out is NULL");
+  *out = nullptr;
+  int count = 0;
+  BACON_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(BACON_INVALID_ARGUMENT, "bacon_ctx_create: no such device");
+  BACON_CUDA(cudaSetDevice(device));
+  bacon_ctx* c = new bacon_ctx();
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&c->d_ctl), 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->h_ctl), 4 * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(BACON_CUDA_ERROR, std::string("bacon_ctx_create: ") + cudaGetErrorString(e));
+  }
+  c->kernels = bacon::all_rk_kernels();
+  *out = c;
+  return BACON_OK;
+}
+
+int bacon_ctx_destroy(bacon_ctx* c) {
+  if (!c) return BACON_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  for (DevBuf* b : {&c->in_y0, &c->in_params, &c->in_t0, &c->in_tend, &c->out_y, &c->out_t,
+                    &c->out_acc, &c->out_rej, &c->out_st, &c->out_tt, &c->out_ty, &c->pl_y, &c->pl_K,
+                    &c->pl_t, &c->pl_dt, &c->pl_end, &c->pl_att, &c->pl_acc, &c->pl_rej, &c->pl_st})
+    b->release();
+  if (c->d_ctl) cudaFree(c->d_ctl);
+  if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return BACON_OK;
+}
+
+int64_t bacon_ctx_kernel_launches(const bacon_ctx* c) { return c ? c->launches : 0; }
+
+// Builder-equivalent checks on a filled problem (src/ivp/rk.rs:168-256).
+int bacon_rk_validate(const bacon_problem* p) {
+  if (!p) return fail(BACON_INVALID_ARGUMENT, "problem is NULL");
+  if (p->n < 0) return fail(BACON_INVALID_ARGUMENT, "n < 0");
+  if (p->dim < 1) return fail(BACON_INVALID_ARGUMENT, "dim < 1");
+  if (p->n > 0 && !p->y0) return fail(BACON_MISSING_PARAMETERS, "initial conditions missing");
+  if (p->tol <= 0.0) return fail(BACON_TOLERANCE_OOB, "tolerance <= 0");
+  if (p->dt_max <= 0.0 || p->dt_min <= 0.0) return fail(BACON_TIME_DELTA_OOB, "dt bound <= 0");
+  if (!p->t0 && !p->t_end && p->t0_scalar >= p->t_end_scalar)
+    return fail(BACON_TIME_END_OOB, "ending time is not after the initial time");
+  const int ed = expected_dim(p->rhs);
+  if (p->rhs < 0 || p->rhs > BACON_RHS_LINEAR) return fail(BACON_INVALID_ARGUMENT, "unknown rhs");
+  if (ed > 0 && p->dim != ed) return fail(BACON_INVALID_ARGUMENT, "dim does not match the rhs");
+  if (p->n_params < expected_params(p->rhs, p->dim))
+    return fail(BACON_INVALID_ARGUMENT, "too few parameters for the rhs");
+  if (p->n > 0 && p->n_params > 0 && !p->params) return fail(BACON_INVALID_ARGUMENT, "params is NULL");
+  return BACON_OK;
+}
+
+int bacon_measure_fp64_peak(bacon_ctx* c, double* gflops) {
+  if (!c || !gflops) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  BACON_CUDA(cudaSetDevice(c->device));
+  const double g = bacon::measure_fp64_fma_gflops(c->stream, c->num_sms);
+  if (g < 0) return fail(BACON_CUDA_ERROR, "fp64 probe failed");
+  c->launches += 4;
+  *gflops = g;
+  return BACON_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Effective dt bounds after the builder's cross-clamping with minimum set
+// before maximum (with_minimum_dt then with_maximum_dt, rk.rs:179-210).
+void clamp_dt(double& dt_min, double dt_max) {
+  if (dt_min > dt_max) dt_min = dt_max;
+}
+
+struct Resolved {
+  const double *y0, *params, *t0, *t_end;
+  double *y_out, *t_out, *traj_t, *traj_y;
+  int32_t *acc, *rej, *st;
+};
+
+int stage_inputs(bacon_ctx* c, const bacon_problem* p, const bacon_rk_result* r, bool host, Resolved& o) {
+  const size_t n = static_cast<size_t>(p->n);
+  const size_t yb = n * p->dim * sizeof(double);
+  if (!host) {
+    o = Resolved{p->y0, p->params, p->t0, p->t_end, r->y_final, r->t_final, r->traj_t, r->traj_y,
+                 r->accepted, r->rejected, r->status};
+    return BACON_OK;
+  }
+  BACON_CUDA(c->in_y0.ensure(yb));
+  BACON_CUDA(c->out_y.ensure(yb));
+  BACON_CUDA(c->out_t.ensure(n * sizeof(double)));
+  BACON_CUDA(c->out_acc.ensure(n * sizeof(int32_t)));
+  BACON_CUDA(c->out_rej.ensure(n * sizeof(int32_t)));
+  BACON_CUDA(c->out_st.ensure(n * sizeof(int32_t)));
+  o.y0 = c->in_y0.as<double>();
+  o.params = nullptr;
+  if (p->n_params > 0 && p->params) {
+    BACON_CUDA(c->in_params.ensure(n * p->n_params * sizeof(double)));
+    o.params = c->in_params.as<double>();
+  }
+  o.t0 = nullptr;
+  o.t_end = nullptr;
+  if (p->t0) {
+    BACON_CUDA(c->in_t0.ensure(n * sizeof(double)));
+    o.t0 = c->in_t0.as<double>();
+  }
+  if (p->t_end) {
+    BACON_CUDA(c->in_tend.ensure(n * sizeof(double)));
+    o.t_end = c->in_tend.as<double>();
+  }
+  o.y_out = c->out_y.as<double>();
+  o.t_out = c->out_t.as<double>();
+  o.acc = c->out_acc.as<int32_t>();
+  o.rej = c->out_rej.as<int32_t>();
+  o.st = c->out_st.as<int32_t>();
+  o.traj_t = nullptr;
+  o.traj_y = nullptr;
+  if (r->traj_t && r->traj_cap > 0) {
+    BACON_CUDA(c->out_tt.ensure(n * r->traj_cap * sizeof(double)));
+    BACON_CUDA(c->out_ty.ensure(n * r->traj_cap * p->dim * sizeof(double)));
+    o.traj_t = c->out_tt.as<double>();
+    o.traj_y = c->out_ty.as<double>();
+  }
+  return BACON_OK;
+}
+
+int enqueue_h2d(bacon_ctx* c, const bacon_problem* p, const Resolved& o) {
+  const size_t n = static_cast<size_t>(p->n);
+  BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(o.y0), p->y0, n * p->dim * sizeof(double),
+                             cudaMemcpyHostToDevice, c->stream));
+  if (o.params)
+    BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(o.params), p->params, n * p->n_params * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+  if (o.t0)
+    BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(o.t0), p->t0, n * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+  if (o.t_end)
+    BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(o.t_end), p->t_end, n * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+  return BACON_OK;
+}
+
+int enqueue_d2h(bacon_ctx* c, const bacon_problem* p, const bacon_rk_result* r, const Resolved& o) {
+  const size_t n = static_cast<size_t>(p->n);
+  BACON_CUDA(cudaMemcpyAsync(r->y_final, o.y_out, n * p->dim * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(r->t_final, o.t_out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(r->accepted, o.acc, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(r->rejected, o.rej, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(r->status, o.st, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  if (o.traj_t) {
+    BACON_CUDA(cudaMemcpyAsync(r->traj_t, o.traj_t, n * r->traj_cap * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+    BACON_CUDA(cudaMemcpyAsync(r->traj_y, o.traj_y, n * r->traj_cap * p->dim * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  }
+  return BACON_OK;
+}
+
+bool is_pinned_or_device(const void* ptr) {
+  if (!ptr) return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+int check_result_ptrs(const bacon_problem* p, const bacon_rk_result* r) {
+  if (!r) return fail(BACON_INVALID_ARGUMENT, "result is NULL");
+  if (p->n > 0 && (!r->y_final || !r->t_final || !r->accepted || !r->rejected || !r->status))
+    return fail(BACON_INVALID_ARGUMENT, "result array is NULL");
+  if ((r->traj_t == nullptr) != (r->traj_y == nullptr))
+    return fail(BACON_INVALID_ARGUMENT, "traj_t and traj_y must be given together");
+  if (r->traj_t && r->traj_cap < 0) return fail(BACON_INVALID_ARGUMENT, "traj_cap < 0");
+  return BACON_OK;
+}
+
+// Reads the lowest failing index and its status after the solve finished.
+int batch_return_code(bacon_ctx* c, const bacon_rk_result* r, bool host, const Resolved& o) {
+  const unsigned long long ff = c->h_ctl[1];
+  if (ff == ~0ull) return BACON_OK;
+  int32_t st = 0;
+  if (host) {
+    st = r->status[ff];
+  } else {
+    BACON_CUDA(cudaMemcpy(&st, o.st + ff, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
+  return fail(st, "system " + std::to_string(ff) + " ended with status " + std::to_string(st));
+}
+
+}  // namespace
+
+extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                              bacon_rk_result* r) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (opt->method != BACON_RK45 && opt->method != BACON_RK23)
+    return fail(BACON_INVALID_ARGUMENT, "unknown method");
+  if (opt->layout < 0 || opt->layout > 2) return fail(BACON_INVALID_ARGUMENT, "unknown layout");
+  if (opt->precision < 0 || opt->precision > 2) return fail(BACON_INVALID_ARGUMENT, "unknown precision");
+  if (p->dyn_dim && p->dim == 4) return fail(BACON_UNSUPPORTED, "dynamic 4-vectors are not compiled");
+  const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
+  const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
+  const void* fn = nullptr;
+  for (const auto& e : c->kernels)
+    if (e.key == key) fn = e.fn;
+  if (!fn) return fail(BACON_UNSUPPORTED, "no compiled kernel for this (method, layout, precision, rhs, dim)");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+
+  double dt_min = p->dt_min;
+  clamp_dt(dt_min, p->dt_max);
+  bacon::RkArgs a{};
+  a.n = p->n;
+  a.y0 = o.y0;
+  a.params = o.params;
+  a.t0 = o.t0;
+  a.t_end = o.t_end;
+  a.t0_s = p->t0_scalar;
+  a.t_end_s = p->t_end_scalar;
+  a.tol = p->tol;
+  a.dt_min = dt_min;
+  a.dt_max = p->dt_max;
+  a.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  a.y_out = o.y_out;
+  a.t_out = o.t_out;
+  a.accepted = o.acc;
+  a.rejected = o.rej;
+  a.status = o.st;
+  a.traj_t = o.traj_t;
+  a.traj_y = o.traj_y;
+  a.traj_cap = (o.traj_t ? r->traj_cap : 0);
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+
+  int block = opt->block > 0 ? opt->block : 128;
+  if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
+  int max_bps = 0;
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
+  if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
+  if (bps > max_bps) bps = max_bps;
+  long long grid = static_cast<long long>(c->num_sms) * bps;
+  const long long need = (p->n + block - 1) / block;
+  if (grid > need) grid = need;
+
+  void* args[] = {&a};
+  bool use_graph = opt->use_graph != 0;
+  if (use_graph && host) {
+    for (const void* q : {static_cast<const void*>(p->y0), static_cast<const void*>(p->params),
+                          static_cast<const void*>(p->t0), static_cast<const void*>(p->t_end),
+                          static_cast<const void*>(r->y_final), static_cast<const void*>(r->t_final),
+                          static_cast<const void*>(r->accepted), static_cast<const void*>(r->rejected),
+                          static_cast<const void*>(r->status), static_cast<const void*>(r->traj_t),
+                          static_cast<const void*>(r->traj_y)})
+      if (!is_pinned_or_device(q)) use_graph = false;
+  }
+
+  auto enqueue_all = [&]() -> int {
+    int e;
+    if (host && (e = enqueue_h2d(c, p, o)) != BACON_OK) return e;
+    BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+    BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+    BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, 0, c->stream));
+    if (host && (e = enqueue_d2h(c, p, r, o)) != BACON_OK) return e;
+    BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c->stream));
+    return BACON_OK;
+  };
+
+  if (use_graph) {
+    uint64_t h = fnv1a(&a, sizeof(a));
+    h = fnv1a(&key, sizeof(key), h);
+    h = fnv1a(&grid, sizeof(grid), h);
+    h = fnv1a(&block, sizeof(block), h);
+    const void* hp[] = {p->y0, p->params, p->t0, p->t_end, r->y_final, r->t_final, r->accepted,
+                        r->rejected, r->status, r->traj_t, r->traj_y};
+    h = fnv1a(hp, sizeof(hp), h);
+    h = fnv1a(&host, sizeof(host), h);
+    auto it = c->graphs.find(h);
+    if (it == c->graphs.end()) {
+      BACON_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      const int e = enqueue_all();
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (e != BACON_OK) {
+        if (g) cudaGraphDestroy(g);
+        return e;
+      }
+      if (ce != cudaSuccess) return fail(BACON_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(ce));
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail(BACON_CUDA_ERROR, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+      it = c->graphs.emplace(h, bacon_ctx::Graph{ex}).first;
+    }
+    BACON_CUDA(cudaGraphLaunch(it->second.exec, c->stream));
+  } else {
+    if ((rc = enqueue_all()) != BACON_OK) return rc;
+  }
+  c->launches += 1;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  return batch_return_code(c, r, host, o);
+}
+
+extern "C" int bacon_rk_solve_plain(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                    bacon_rk_result* r) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (opt->precision != BACON_FP64_EXACT) return fail(BACON_UNSUPPORTED, "the plain baseline is FP64 exact only");
+  if (r->traj_t) return fail(BACON_UNSUPPORTED, "the plain baseline records no trajectory");
+  if (p->dyn_dim && p->dim == 4) return fail(BACON_UNSUPPORTED, "dynamic 4-vectors are not compiled");
+  const void* fn = bacon::plain_kernel(p->rhs, p->dim);
+  if (!fn) return fail(BACON_UNSUPPORTED, "no plain kernel for this (rhs, dim)");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+
+  bacon::PlainTables tb{};
+  bacon::plain_tables(opt->method, (opt->method == BACON_RK23 && opt->layout == 2) ? 1 : opt->layout, tb);
+  BACON_CUDA(bacon::plain_upload_tables(tb, c->stream));
+  const size_t n = static_cast<size_t>(p->n);
+  const int S = tb.stages;
+  BACON_CUDA(c->pl_K.ensure(n * S * p->dim * sizeof(double)));
+  BACON_CUDA(c->pl_dt.ensure(n * sizeof(double)));
+  BACON_CUDA(c->pl_end.ensure(n * sizeof(double)));
+  BACON_CUDA(c->pl_att.ensure(n * sizeof(int64_t)));
+
+  double dt_min = p->dt_min;
+  clamp_dt(dt_min, p->dt_max);
+  bacon::PlainArgs st{};
+  st.n = p->n;
+  st.stages = S;
+  st.dim = p->dim;
+  st.y = o.y_out;  // the state array doubles as the output
+  st.K = c->pl_K.as<double>();
+  st.t = o.t_out;
+  st.dt = c->pl_dt.as<double>();
+  st.end = c->pl_end.as<double>();
+  st.attempts = c->pl_att.as<int64_t>();
+  st.accepted = o.acc;
+  st.rejected = o.rej;
+  st.status = o.st;
+  st.params = o.params;
+  st.live = reinterpret_cast<unsigned int*>(c->d_ctl + 2);
+  st.tol = p->tol;
+  st.dt_min = dt_min;
+  st.dt_max = p->dt_max;
+  st.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+
+  bacon::PlainInitArgs ia{};
+  ia.n = p->n;
+  ia.dim = p->dim;
+  ia.stages = S;
+  ia.y0 = o.y0;
+  ia.t0 = o.t0;
+  ia.t_end = o.t_end;
+  ia.t0_s = p->t0_scalar;
+  ia.t_end_s = p->t_end_scalar;
+  ia.dt0 = (p->dt_max + dt_min) * 0.5;
+  ia.st = st;
+  const int block = opt->block > 0 ? opt->block : 256;
+  const unsigned grid = static_cast<unsigned>((p->n + block - 1) / block);
+  void* iargs[] = {&ia};
+  BACON_CUDA(cudaLaunchKernel(bacon::plain_init_kernel(), dim3(grid), dim3(block), iargs, 0, c->stream));
+  c->launches += 1;
+  void* sargs[] = {&st};
+  unsigned int* h_live = reinterpret_cast<unsigned int*>(c->h_ctl + 2);
+  for (;;) {
+    BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
+    BACON_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(block), sargs, 0, c->stream));
+    c->launches += 1;
+    BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaStreamSynchronize(c->stream));
+    if (*h_live == 0) break;
+  }
+  BACON_CUDA(cudaGetLastError());
+  if (host && (rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  // Lowest failing index: scan the statuses on the host.
+  std::vector<int32_t> hs;
+  const int32_t* sp = r->status;
+  if (!host) {
+    hs.resize(n);
+    BACON_CUDA(cudaMemcpy(hs.data(), o.st, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    sp = hs.data();
+  }
+  for (size_t i = 0; i < n; ++i)
+    if (sp[i] != 0) return fail(sp[i], "system " + std::to_string(i) + " ended with status " + std::to_string(sp[i]));
+  return BACON_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Builder mirror of the IVPSolver trait (src/ivp.rs:134-190,
+// src/ivp/rk.rs:136-247, src/ivp/bdf.rs:144-255).
+struct bacon_builder {
+  int32_t kind = 0;
+  int32_t dim = 0;
+  bool dyn = false;
+  bool has_dt_max = false, has_dt_min = false, has_t0 = false, has_end = false, has_tol = false;
+  double dt_max = 0, dt_min = 0, t0 = 0, t_end = 0, tol = 0;
+  std::vector<double> y0;
+  int64_t n = 0;
+  bool has_y0 = false;
+  int32_t rhs = -1;
+  std::vector<double> params;
+  int32_t n_params = 0;
+  std::vector<double> t_ends;
+};
+
+extern "C" {
+
+int bacon_builder_new(int32_t kind, int32_t dim, bacon_builder** out) {
+  if (!out) return fail(BACON_INVALID_ARGUMENT, "out is NULL");
+  if (kind < 0 || kind > 3 || dim < 1) return fail(BACON_INVALID_ARGUMENT, "bad kind or dim");
+  *out = new bacon_builder();
+  (*out)->kind = kind;
+  (*out)->dim = dim;
+  return BACON_OK;
+}
+
+int bacon_builder_new_dyn(int32_t kind, int32_t size, bacon_builder** out) {
+  const int rc = bacon_builder_new(kind, size, out);
+  if (rc == BACON_OK) (*out)->dyn = true;
+  return rc;
+}
+
+void bacon_builder_free(bacon_builder* b) { delete b; }
+
+int bacon_builder_with_tolerance(bacon_builder* b, double tol) {
+  if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  if (tol <= 0.0) return fail(BACON_TOLERANCE_OOB, "the provided tolerance was out-of-bounds");
+  b->tol = tol;
+  b->has_tol = true;
+  return BACON_OK;
+}
+
+int bacon_builder_with_maximum_dt(bacon_builder* b, double max) {
+  if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  if (max <= 0.0) return fail(BACON_TIME_DELTA_OOB, "the provided time delta was out-of-bounds");
+  b->dt_max = max;
+  b->has_dt_max = true;
+  if (b->has_dt_min && b->dt_min > max) b->dt_min = max;
+  return BACON_OK;
+}
+
+int bacon_builder_with_minimum_dt(bacon_builder* b, double min) {
+  if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  if (min <= 0.0) return fail(BACON_TIME_DELTA_OOB, "the provided time delta was out-of-bounds");
+  b->dt_min = min;
+  b->has_dt_min = true;
+  if (b->has_dt_max && b->dt_max < min) b->dt_max = min;
+  return BACON_OK;
+}
+
+int bacon_builder_with_initial_time(bacon_builder* b, double initial) {
+  if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  b->t0 = initial;
+  b->has_t0 = true;
+  if (b->has_end && b->t_end <= initial)
+    return fail(BACON_TIME_START_OOB, "the provided starting time was after the provided ending time");
+  for (double e : b->t_ends)
+    if (e <= initial) return fail(BACON_TIME_START_OOB, "the provided starting time was after an ending time");
+  return BACON_OK;
+}
+
+int bacon_builder_with_ending_time(bacon_builder* b, double ending) {
+  if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  b->t_end = ending;
+  b->has_end = true;
+  b->t_ends.clear();
+  if (b->has_t0 && b->t0 >= ending)
+    return fail(BACON_TIME_END_OOB, "the provided ending time was before the provided starting time");
+  return BACON_OK;
+}
+
+int bacon_builder_with_ending_times(bacon_builder* b, const double* t_end, int64_t n) {
+  if (!b || (!t_end && n > 0) || n < 0) return fail(BACON_INVALID_ARGUMENT, "bad arguments");
+  b->t_ends.assign(t_end, t_end + n);
+  b->has_end = true;
+  if (b->has_t0)
+    for (int64_t i = 0; i < n; ++i)
+      if (b->t0 >= t_end[i])
+        return fail(BACON_TIME_END_OOB, "ending time of system " + std::to_string(i) + " is not after the start");
+  return BACON_OK;
+}
+
+int bacon_builder_with_initial_conditions(bacon_builder* b, const double* y0, int64_t n) {
+  if (!b || (!y0 && n > 0) || n < 0) return fail(BACON_INVALID_ARGUMENT, "bad arguments");
+  b->y0.assign(y0, y0 + static_cast<size_t>(n) * b->dim);
+  b->n = n;
+  b->has_y0 = true;
+  return BACON_OK;
+}
+
+int bacon_builder_with_derivative(bacon_builder* b, int32_t rhs, const double* params, int32_t n_params) {
+  if (!b || n_params < 0 || (n_params > 0 && !params)) return fail(BACON_INVALID_ARGUMENT, "bad arguments");
+  if (rhs < 0 || rhs > BACON_RHS_LINEAR) return fail(BACON_INVALID_ARGUMENT, "unknown rhs");
+  b->rhs = rhs;
+  b->n_params = n_params;
+  b->params.clear();
+  if (n_params > 0) {
+    if (!b->has_y0) return fail(BACON_INVALID_ARGUMENT, "set initial conditions before per-system parameters");
+    b->params.assign(params, params + static_cast<size_t>(n_params) * b->n);
+  }
+  return BACON_OK;
+}
+
+int bacon_builder_problem(const bacon_builder* b, bacon_problem* out) {
+  if (!b || !out) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  // rk.rs:250-256 / bdf.rs:258-264: every parameter must have been set.
+  if (!b->has_dt_max || !b->has_dt_min || !b->has_tol || !b->has_t0 || !b->has_end || !b->has_y0 || b->rhs < 0)
+    return fail(BACON_MISSING_PARAMETERS, "the solver does not have all required parameters set");
+  if (!b->t_ends.empty() && static_cast<int64_t>(b->t_ends.size()) != b->n)
+    return fail(BACON_INVALID_ARGUMENT, "ending times and initial conditions disagree in length");
+  std::memset(out, 0, sizeof(*out));
+  out->n = b->n;
+  out->dim = b->dim;
+  out->rhs = b->rhs;
+  out->n_params = b->n_params;
+  out->dyn_dim = b->dyn ? 1 : 0;
+  out->y0 = b->y0.data();
+  out->params = b->n_params > 0 ? b->params.data() : nullptr;
+  out->t0 = nullptr;
+  out->t_end = b->t_ends.empty() ? nullptr : b->t_ends.data();
+  out->t0_scalar = b->t0;
+  out->t_end_scalar = b->t_ends.empty() ? b->t_end : 0.0;
+  if (!b->t_ends.empty()) out->t_end_scalar = b->t0 + 1.0;  // unused: per-system ends given
+  out->tol = b->tol;
+  out->dt_min = b->dt_min;
+  out->dt_max = b->dt_max;
+  return BACON_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Kernel registry: every compiled (method, layout, precision, rhs, dim)
+// combination of the persistent Runge-Kutta kernel, looked up at solve time.
+#pragma once
+
+#include <vector>
+
+namespace bacon {
+
+struct RkKey {
+  int method;     // 0 RK45, 1 RK23
+  int layout;     // 0 as_compiled, 1 as_written, 2 fehlberg
+  int precision;  // 0 fp64 exact, 1 fp64 fma, 2 fp32 compensated
+  int rhs;
+  int dim;
+  bool operator==(const RkKey& o) const {
+    return method == o.method && layout == o.layout && precision == o.precision && rhs == o.rhs &&
+           dim == o.dim;
+  }
+};
+
+struct RkEntry {
+  RkKey key;
+  const void* fn;  // __global__ void(RkArgs)
+};
+
+void register_rk45_exact_l0(std::vector<RkEntry>& v);
+void register_rk45_exact_l1(std::vector<RkEntry>& v);
+void register_rk45_exact_l2(std::vector<RkEntry>& v);
+void register_rk45_fma(std::vector<RkEntry>& v);
+void register_rk23(std::vector<RkEntry>& v);
+
+inline std::vector<RkEntry> all_rk_kernels() {
+  std::vector<RkEntry> v;
+  register_rk45_exact_l0(v);
+  register_rk45_exact_l1(v);
+  register_rk45_exact_l2(v);
+  register_rk45_fma(v);
+  register_rk23(v);
+  return v;
+}
+
+}  // namespace bacon

@@ -1,0 +1,207 @@
+"""Low-level batched solves over the C ABI.
+
+``rk_solve`` accepts either host numpy arrays (the library stages them
+through device memory: BACON_MEM_HOST) or CUDA tensors that are already
+resident on the GPU (BACON_MEM_DEVICE).  Arrays are SoA: ``y0`` is
+(dim, n), ``params`` is (n_params, n).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Any
+
+import numpy as np
+
+from . import _capi
+
+RK45, RK23 = 0, 1
+AS_COMPILED, AS_WRITTEN, FEHLBERG = 0, 1, 2
+FP64_EXACT, FP64_FMA, FP32_COMP = 0, 1, 2
+MEM_DEVICE, MEM_HOST = 0, 1
+
+
+class IVPError(Exception):
+    """An IVPError variant (src/ivp.rs:50-76) or an engine extension code."""
+
+    def __init__(self, code: int, message: str = ""):
+        self.code = int(code)
+        self.variant = _capi.STATUS_NAMES.get(self.code, f"Status{self.code}")
+        super().__init__(f"{self.variant}: {message}" if message else self.variant)
+
+
+def check(code: int) -> None:
+    if code != 0:
+        raise IVPError(code, _capi.last_error())
+
+
+class Context:
+    """Owns a bacon_ctx (stream, scratch, graph and tuning caches) on one device."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _capi.load()
+        h = ctypes.c_void_p()
+        check(self._lib.bacon_ctx_create(int(device), ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self._lib.bacon_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._lib.bacon_ctx_kernel_launches(self.handle))
+
+    def fp64_peak_gflops(self) -> float:
+        g = ctypes.c_double()
+        check(self._lib.bacon_measure_fp64_peak(self.handle, ctypes.byref(g)))
+        return g.value
+
+
+_default: dict[int, Context] = {}
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default:
+        _default[device] = Context(device)
+    return _default[device]
+
+
+@dataclass
+class Solution:
+    """Per-system outcome of a batched solve (host arrays or CUDA tensors)."""
+    y: Any            # (dim, n)
+    t: Any            # (n,)
+    accepted: Any     # (n,)
+    rejected: Any     # (n,)
+    status: Any       # (n,)
+    code: int         # BACON_OK or the lowest failing system's status
+    traj_t: Any = None
+    traj_y: Any = None
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _is_device(a) -> bool:
+    return not isinstance(a, np.ndarray) and getattr(a, "is_cuda", False)
+
+
+def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False):
+    """Build a bacon_problem; t0 / t_end may be scalars or per-system arrays."""
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    p = _capi.Problem()
+    p.n = n
+    p.dim = dim
+    p.rhs = int(rhs)
+    p.n_params = 0 if params is None else int(params.shape[0])
+    p.dyn_dim = int(bool(dyn_dim))
+    p.y0 = _ptr(y0)
+    p.params = _ptr(params) if p.n_params else None
+    if np.isscalar(t0):
+        p.t0 = None
+        p.t0_scalar = float(t0)
+    else:
+        p.t0 = _ptr(t0)
+    if np.isscalar(t_end):
+        p.t_end = None
+        p.t_end_scalar = float(t_end)
+    else:
+        p.t_end = _ptr(t_end)
+    p.shared = None
+    p.tol, p.dt_min, p.dt_max = float(tol), float(dt_min), float(dt_max)
+    return p
+
+
+def rk_options(method=RK45, layout=FEHLBERG, precision=FP64_EXACT, memory=MEM_HOST, max_attempts=0,
+               block=0, blocks_per_sm=0, use_graph=True):
+    o = _capi.RkOptions()
+    o.method, o.layout, o.precision, o.memory = method, layout, precision, memory
+    o.max_attempts = int(max_attempts)
+    o.block, o.blocks_per_sm = int(block), int(blocks_per_sm)
+    o.use_graph = int(bool(use_graph))
+    return o
+
+
+def alloc_outputs(dim: int, n: int, device: bool, traj_cap: int = 0, pin: bool = False):
+    if device:
+        import torch
+        dev = torch.device("cuda")
+        out = dict(y=torch.empty((dim, n), dtype=torch.float64, device=dev),
+                   t=torch.empty(n, dtype=torch.float64, device=dev),
+                   accepted=torch.empty(n, dtype=torch.int32, device=dev),
+                   rejected=torch.empty(n, dtype=torch.int32, device=dev),
+                   status=torch.empty(n, dtype=torch.int32, device=dev))
+        if traj_cap:
+            out["traj_t"] = torch.empty((n, traj_cap), dtype=torch.float64, device=dev)
+            out["traj_y"] = torch.empty((n, traj_cap, dim), dtype=torch.float64, device=dev)
+        return out
+    if pin:
+        import torch
+        def mk(shape, dt):
+            return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+        f64, i32 = torch.float64, torch.int32
+    else:
+        def mk(shape, dt):
+            return np.empty(shape, dtype=dt)
+        f64, i32 = np.float64, np.int32
+    out = dict(y=mk((dim, n), f64), t=mk(n, f64), accepted=mk(n, i32), rejected=mk(n, i32),
+               status=mk(n, i32))
+    if traj_cap:
+        out["traj_t"] = mk((n, traj_cap), f64)
+        out["traj_y"] = mk((n, traj_cap, dim), f64)
+    return out
+
+
+def make_result(out, traj_cap=0):
+    r = _capi.RkResult()
+    r.y_final, r.t_final = _ptr(out["y"]), _ptr(out["t"])
+    r.accepted, r.rejected, r.status = _ptr(out["accepted"]), _ptr(out["rejected"]), _ptr(out["status"])
+    r.traj_t = _ptr(out.get("traj_t"))
+    r.traj_y = _ptr(out.get("traj_y"))
+    r.traj_cap = int(traj_cap)
+    return r
+
+
+def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
+             precision=FP64_EXACT, max_attempts=0, traj_cap=0, ctx: Context | None = None,
+             plain=False, block=0, blocks_per_sm=0, use_graph=True, dyn_dim=False, out=None,
+             raise_on_error=False) -> Solution:
+    """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors."""
+    ctx = ctx or default_context()
+    device = _is_device(y0)
+    if not device:
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        if params is not None:
+            params = np.ascontiguousarray(params, dtype=np.float64)
+        if not np.isscalar(t0):
+            t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        if not np.isscalar(t_end):
+            t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim)
+    opts = rk_options(method, layout, precision, MEM_DEVICE if device else MEM_HOST, max_attempts,
+                      block, blocks_per_sm, use_graph)
+    if out is None:
+        out = alloc_outputs(dim, n, device, traj_cap)
+    res = make_result(out, traj_cap)
+    lib = _capi.load()
+    fn = lib.bacon_rk_solve_plain if plain else lib.bacon_rk_solve
+    code = fn(ctx.handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res))
+    if code in (14, 15, 16) or (raise_on_error and code != 0):
+        raise IVPError(code, _capi.last_error())
+    return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code),
+                    out.get("traj_t"), out.get("traj_y"))

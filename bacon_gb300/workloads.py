@@ -1,0 +1,94 @@
+"""Seeded synthetic batches for the five benchmark workloads.
+
+The reference (aftix/bacon) publishes no benchmark inputs, so every batch is
+generated here from a fixed numpy seed with the shapes and value
+distributions of the workload description.  Arrays are SoA: ``y0`` is
+(dim, n), ``params`` is (n_params, n).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+RHS_EXP, RHS_DECAY, RHS_QUADRATIC, RHS_SINE, RHS_HARMONIC = 0, 1, 2, 3, 4
+RHS_VDP, RHS_LORENZ, RHS_LOTKA, RHS_ROBERTSON, RHS_CHAIN, RHS_LINEAR = 5, 6, 7, 8, 9, 10
+
+
+@dataclass
+class Batch:
+    name: str
+    rhs: int
+    y0: np.ndarray          # (dim, n)
+    params: np.ndarray      # (n_params, n)
+    t0: np.ndarray          # (n,)
+    t_end: np.ndarray       # (n,)
+    tol: float
+    dt_min: float
+    dt_max: float
+    seed: int
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return self.y0.shape[1]
+
+    @property
+    def dim(self) -> int:
+        return self.y0.shape[0]
+
+    def subset(self, idx) -> "Batch":
+        idx = np.asarray(idx)
+        return Batch(self.name, self.rhs, np.ascontiguousarray(self.y0[:, idx]),
+                     np.ascontiguousarray(self.params[:, idx]), self.t0[idx].copy(),
+                     self.t_end[idx].copy(), self.tol, self.dt_min, self.dt_max, self.seed,
+                     dict(self.extra))
+
+
+def van_der_pol(n: int = 4096, seed: int = 1) -> Batch:
+    """4096 Van der Pol oscillators y'' = mu (1 - y^2) y' - y as 2-dim systems:
+    mu ~ U[0.1, 2], y0 ~ U[-2, 2]^2, t in [0, 10], tol 1e-6, dt in [1e-6, 0.1]."""
+    rng = np.random.default_rng(seed)
+    mu = rng.uniform(0.1, 2.0, n)
+    y0 = rng.uniform(-2.0, 2.0, (2, n))
+    return Batch("van_der_pol", RHS_VDP, y0, mu[None, :].copy(), np.zeros(n), np.full(n, 10.0),
+                 1e-6, 1e-6, 0.1, seed)
+
+
+def lorenz(n: int = 1 << 20, seed: int = 2) -> Batch:
+    """Lorenz-63 batch: sigma ~ U[9, 11], rho ~ U[20, 30], beta ~ U[2.4, 2.9],
+    y0 ~ N(0, 5^2 I), end time T ~ U[1, 20] (uneven work), tol 1e-6.
+    dt bounds are not given by the workload; dt_min 1e-8, dt_max 0.1 chosen."""
+    rng = np.random.default_rng(seed)
+    sigma = rng.uniform(9.0, 11.0, n)
+    rho = rng.uniform(20.0, 30.0, n)
+    beta = rng.uniform(2.4, 2.9, n)
+    y0 = rng.normal(0.0, 5.0, (3, n))
+    t_end = rng.uniform(1.0, 20.0, n)
+    return Batch("lorenz", RHS_LORENZ, y0, np.stack([sigma, rho, beta]), np.zeros(n), t_end,
+                 1e-6, 1e-8, 0.1, seed)
+
+
+def lotka_volterra(n: int = 1 << 18, seed: int = 3) -> Batch:
+    """Lotka-Volterra dx = a x - b x y, dy = c x y - d y: a,b,c,d ~ U[0.5, 1.5],
+    y0 ~ U[0.5, 2]^2, t in [0, 15], tol 1e-7, target ~ U[0.5, 2]^2.
+    dt bounds chosen: dt_min 1e-8, dt_max 0.1."""
+    rng = np.random.default_rng(seed)
+    prm = rng.uniform(0.5, 1.5, (4, n))
+    y0 = rng.uniform(0.5, 2.0, (2, n))
+    target = rng.uniform(0.5, 2.0, (2, n))
+    return Batch("lotka_volterra", RHS_LOTKA, y0, prm, np.zeros(n), np.full(n, 15.0),
+                 1e-7, 1e-8, 0.1, seed, {"target": target, "checkpoint_every": 32})
+
+
+def robertson(n: int = 1 << 16, seed: int = 5) -> Batch:
+    """Robertson kinetics: k1 ~ 1e-2 U[2,6], k2 ~ 1e7 U[1,5], k3 ~ 1e4 U[0.5,2],
+    y0 = (1, 0, 0), t in [0, 1e4], tol 1e-6; dt bounds chosen 1e-10 .. 1e3."""
+    rng = np.random.default_rng(seed)
+    k1 = 1e-2 * rng.uniform(2.0, 6.0, n)
+    k2 = 1e7 * rng.uniform(1.0, 5.0, n)
+    k3 = 1e4 * rng.uniform(0.5, 2.0, n)
+    y0 = np.zeros((3, n))
+    y0[0] = 1.0
+    return Batch("robertson", RHS_ROBERTSON, y0, np.stack([k1, k2, k3]), np.zeros(n),
+                 np.full(n, 1e4), 1e-6, 1e-10, 1e3, seed)

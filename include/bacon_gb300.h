@@ -1,0 +1,219 @@
+/*
+ * bacon_gb300 — C ABI of the GB300 (sm_103a) batched initial-value-problem
+ * engine.  It replaces, for batches of independent systems, the solver API of
+ * the Rust crate bacon-sci 0.16.2 (aftix/bacon):
+ *
+ *   IVPSolver builder trait            src/ivp.rs:134-190
+ *   RungeKutta builder impl            src/ivp/rk.rs:118-344
+ *   RungeKuttaSolver::step             src/ivp/rk.rs:361-423
+ *   IVPIterator::next / collect_vec    src/ivp.rs:192-239
+ *   BDF builder / BDFSolver::step      src/ivp/bdf.rs:124-332, :495-634
+ *   IVPError                           src/ivp.rs:50-76
+ *
+ * All entry points are plain C: pointers, sizes and status codes.  Every
+ * function returns a bacon_status; bacon_last_error() gives a message for the
+ * calling thread's last failure.  Calls on one bacon_ctx must not overlap
+ * (the reference solvers are single-threaded objects, src/ivp.rs:102-125);
+ * separate contexts may be used from separate threads.
+ */
+#ifndef BACON_GB300_H
+#define BACON_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+/* 1..12 are the IVPError variants in declaration order (src/ivp.rs:50-76).
+ * 13.. are extensions of the batched engine. */
+typedef enum {
+  BACON_OK = 0,
+  BACON_MISSING_PARAMETERS = 1,
+  BACON_USER_ERROR = 2,
+  BACON_TOLERANCE_OOB = 3,
+  BACON_TIME_DELTA_OOB = 4,
+  BACON_TIME_END_OOB = 5,
+  BACON_TIME_START_OOB = 6,
+  BACON_FROM_PRIMITIVE_FAILURE = 7,
+  BACON_MINIMUM_TIME_DELTA_EXCEEDED = 8,
+  BACON_MAXIMUM_ITERATIONS_EXCEEDED = 9,
+  BACON_SINGULAR_MATRIX = 10,
+  BACON_DYNAMIC_ON_STATIC = 11,
+  BACON_STATIC_ON_DYNAMIC = 12,
+  /* A system reached the attempt cap.  The reference has no cap and loops
+   * forever on a NaN error (rk.rs:392-421); the engine stops instead. */
+  BACON_MAX_ATTEMPTS_EXCEEDED = 13,
+  BACON_CUDA_ERROR = 14,
+  BACON_INVALID_ARGUMENT = 15,
+  BACON_UNSUPPORTED = 16
+} bacon_status;
+
+/* ---- right-hand sides --------------------------------------------------- */
+/* The reference takes an arbitrary Rust closure (src/ivp.rs:34-48).  Device
+ * code cannot call host closures, so the engine carries a registry of device
+ * right-hand sides, each with per-system parameters (SoA). */
+typedef enum {
+  BACON_RHS_EXP = 0,        /* y' = y              any dim, 0 params       */
+  BACON_RHS_DECAY = 1,      /* y' = -y             any dim, 0 params       */
+  BACON_RHS_QUADRATIC = 2,  /* y' = -2 t           any dim, 0 params       */
+  BACON_RHS_SINE = 3,       /* y' = cos t          any dim, 0 params       */
+  BACON_RHS_HARMONIC = 4,   /* (y1, -y0)           dim 2,   0 params       */
+  BACON_RHS_VDP = 5,        /* Van der Pol         dim 2,   (mu)           */
+  BACON_RHS_LORENZ = 6,     /* Lorenz-63           dim 3,   (sigma,rho,beta) */
+  BACON_RHS_LOTKA = 7,      /* Lotka-Volterra      dim 2,   (a,b,c,d)      */
+  BACON_RHS_ROBERTSON = 8,  /* Robertson kinetics  dim 3,   (k1,k2,k3)     */
+  BACON_RHS_CHAIN = 9,      /* spring-mass chain   dim 2n,  (k_0..k_{n-1}, c) */
+  BACON_RHS_LINEAR = 10     /* y' = A y, one shared dense A                */
+} bacon_rhs;
+
+/* ---- methods and variants ---------------------------------------------- */
+typedef enum { BACON_RK45 = 0, BACON_RK23 = 1 } bacon_rk_method;
+
+/* Butcher-matrix variants of the reference tableaux.
+ * AS_COMPILED: nalgebra's from_vec fills column-major (src/ivp/rk.rs:459,
+ *   :580) and the step reads row_iter (:370), so stage i uses column i of the
+ *   literal — stage values from the previous attempt.
+ * AS_WRITTEN: the literal read row by row.
+ * FEHLBERG: AS_WRITTEN with the literal 1859/4014 (rk.rs:499) replaced by
+ *   Fehlberg's 1859/4104.  For RK23 it equals AS_WRITTEN. */
+typedef enum {
+  BACON_LAYOUT_AS_COMPILED = 0,
+  BACON_LAYOUT_AS_WRITTEN = 1,
+  BACON_LAYOUT_FEHLBERG = 2
+} bacon_layout;
+
+/* FP64_EXACT: every product and sum separately rounded in the reference's
+ *   order (bit-identical to the CPU restatement).  FP64_FMA: same algorithm,
+ *   products and sums contracted into fused multiply-adds.  FP32_COMP: stages
+ *   in single precision with compensated (error-free) accumulation of y and of
+ *   the error vector; error norm and step control in FP64. */
+typedef enum {
+  BACON_FP64_EXACT = 0,
+  BACON_FP64_FMA = 1,
+  BACON_FP32_COMP = 2
+} bacon_precision;
+
+typedef enum { BACON_MEM_DEVICE = 0, BACON_MEM_HOST = 1 } bacon_memory;
+
+/* ---- context ----------------------------------------------------------- */
+typedef struct bacon_ctx bacon_ctx;
+
+/* Create a context on CUDA device `device`: a stream, the scratch buffers of
+ * the work queue, the autotune cache and the CUDA-graph cache. */
+int bacon_ctx_create(int device, bacon_ctx** out);
+int bacon_ctx_destroy(bacon_ctx* ctx);
+/* Message of the calling thread's last failed call ("" if none). */
+const char* bacon_last_error(void);
+/* Number of kernels the context launched since creation (diagnostics). */
+int64_t bacon_ctx_kernel_launches(const bacon_ctx* ctx);
+
+/* ---- batch description -------------------------------------------------- */
+/* One solve of n independent systems of dimension `dim`.  All arrays are SoA
+ * (component-major): y0[d*n + i], params[k*n + i].  t0 / t_end may be NULL, in
+ * which case the scalars apply to every system (the reference builder takes
+ * scalars, src/ivp/rk.rs:212-234; per-system arrays are the batched
+ * extension for uneven end times). */
+typedef struct {
+  int64_t n;
+  int32_t dim;
+  int32_t rhs;            /* bacon_rhs */
+  int32_t n_params;
+  int32_t dyn_dim;        /* 1: systems are nalgebra Dyn vectors (norm order) */
+  const double* y0;       /* [dim][n] */
+  const double* params;   /* [n_params][n] or NULL */
+  const double* t0;       /* [n] or NULL */
+  const double* t_end;    /* [n] or NULL */
+  const double* shared;   /* BACON_RHS_LINEAR: row-major dim x dim, else NULL */
+  double t0_scalar;
+  double t_end_scalar;
+  double tol;             /* with_tolerance        (rk.rs:168-174) */
+  double dt_min;          /* with_minimum_dt       (rk.rs:197-210) */
+  double dt_max;          /* with_maximum_dt       (rk.rs:179-192) */
+} bacon_problem;
+
+typedef struct {
+  int32_t method;         /* bacon_rk_method */
+  int32_t layout;         /* bacon_layout */
+  int32_t precision;      /* bacon_precision */
+  int32_t memory;         /* bacon_memory: where every array lives */
+  int64_t max_attempts;   /* cap on attempts per system, 0 = 10,000,000 */
+  int32_t block;          /* threads per block, 0 = autotuned */
+  int32_t blocks_per_sm;  /* persistent CTAs per SM, 0 = autotuned */
+  int32_t use_graph;      /* 1: launch through a cached CUDA graph */
+  int32_t reserved;
+} bacon_rk_options;
+
+/* Outputs, same memory kind as the inputs.  (t_final, y_final) is the last
+ * item the reference iterator would yield ((t0, y0) if none); `accepted` is
+ * the number of items it yields, `rejected` the number of Redo results
+ * (src/ivp.rs:227-237); status is 0 when the iterator ended with Done, else
+ * the error it returned.  traj_t/traj_y (optional, NULL to skip) receive the
+ * first traj_cap yielded items per system: traj_t[i*cap + k],
+ * traj_y[(i*cap + k)*dim + d]. */
+typedef struct {
+  double* y_final;        /* [dim][n] */
+  double* t_final;        /* [n] */
+  int32_t* accepted;      /* [n] */
+  int32_t* rejected;      /* [n] */
+  int32_t* status;        /* [n] */
+  double* traj_t;         /* [n][traj_cap] or NULL */
+  double* traj_y;         /* [n][traj_cap][dim] or NULL */
+  int32_t traj_cap;
+  int32_t reserved;
+} bacon_rk_result;
+
+/* Batched RungeKutta45 / RungeKutta23 solve (persistent kernel).  Returns
+ * BACON_OK if every system ended with Done, otherwise the status of the
+ * lowest-index system that failed (per-system codes are in result->status),
+ * or an argument / CUDA error.  Replaces RungeKutta::solve + collect_vec
+ * (src/ivp/rk.rs:249-343, src/ivp.rs:209-211) for each system. */
+int bacon_rk_solve(bacon_ctx* ctx, const bacon_problem* problem,
+                   const bacon_rk_options* options, bacon_rk_result* result);
+
+/* The same solve with the plain one-launch-per-attempt GPU baseline (state,
+ * t and dt in HBM, host loop until every system is done).  Same results. */
+int bacon_rk_solve_plain(bacon_ctx* ctx, const bacon_problem* problem,
+                         const bacon_rk_options* options,
+                         bacon_rk_result* result);
+
+/* Validate a problem the way the reference builder does (rk.rs:168-256):
+ * tolerance, dt bounds, start/end order, missing parameters.  No GPU work. */
+int bacon_rk_validate(const bacon_problem* problem);
+
+/* ---- builder (mirrors the IVPSolver trait, src/ivp.rs:134-190) ---------- */
+typedef struct bacon_builder bacon_builder;
+
+/* kind: 0 = RungeKutta45, 1 = RungeKutta23, 2 = BDF6, 3 = BDF2.
+ * bacon_builder_new mirrors IVPSolver::new (static dimension `dim`);
+ * bacon_builder_new_dyn mirrors new_dyn(size). */
+int bacon_builder_new(int32_t kind, int32_t dim, bacon_builder** out);
+int bacon_builder_new_dyn(int32_t kind, int32_t size, bacon_builder** out);
+void bacon_builder_free(bacon_builder* b);
+int bacon_builder_with_tolerance(bacon_builder* b, double tol);
+int bacon_builder_with_maximum_dt(bacon_builder* b, double max);
+int bacon_builder_with_minimum_dt(bacon_builder* b, double min);
+int bacon_builder_with_initial_time(bacon_builder* b, double initial);
+int bacon_builder_with_ending_time(bacon_builder* b, double ending);
+/* Batched initial conditions, SoA [dim][n] (with_initial_conditions_slice
+ * for n systems at once). */
+int bacon_builder_with_initial_conditions(bacon_builder* b, const double* y0, int64_t n);
+/* with_derivative: a registry right-hand side plus per-system parameters. */
+int bacon_builder_with_derivative(bacon_builder* b, int32_t rhs, const double* params,
+                                  int32_t n_params);
+/* Batched extension: per-system end times (host array of n). */
+int bacon_builder_with_ending_times(bacon_builder* b, const double* t_end, int64_t n);
+/* Fill a bacon_problem from the builder (MissingParameters if incomplete,
+ * rk.rs:250-256).  Pointers in the problem alias the builder's host copies. */
+int bacon_builder_problem(const bacon_builder* b, bacon_problem* out);
+
+/* ---- diagnostics --------------------------------------------------------- */
+/* Measured FP64 fused-multiply-add throughput of the current device in
+ * GFLOP/s (2 flops per DFMA), from a register-resident microbenchmark. */
+int bacon_measure_fp64_peak(bacon_ctx* ctx, double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,197 @@
+"""CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+ctypes wrapper over ``oracle/_build/liboracle.so``, the C restatement of the
+bacon-sci 0.16.2 IVP solvers (src/ivp/rk.rs, src/ivp/bdf.rs).  Only the test
+suite, the smoke check and the benchmark's CPU-baseline leg may import this
+module; the product package never does.  Parity status of the restatement is
+described in oracle/oracle.h ("parity unpinned" at the bit level: the Rust
+reference cannot be built here).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+
+RK45, RK23 = 0, 1
+AS_COMPILED, AS_WRITTEN, FEHLBERG = 0, 1, 2
+POW_QRT, POW_LIBM = 0, 1
+BDF6, BDF2 = 0, 1
+BDF_AS_COMPILED, BDF_CORRECTED = 0, 1
+
+
+class _RkCfg(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32),
+        ("layout", ctypes.c_int32),
+        ("pow_mode", ctypes.c_int32),
+        ("dyn_dim", ctypes.c_int32),
+        ("max_attempts", ctypes.c_int64),
+        ("tol", ctypes.c_double),
+        ("dt_min", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+    ]
+
+
+class _BdfCfg(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("dyn_dim", ctypes.c_int32),
+        ("max_iter", ctypes.c_int32),
+        ("max_steps", ctypes.c_int64),
+        ("tol", ctypes.c_double),
+        ("dt_min", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    srcs = [os.path.join(_HERE, f) for f in os.listdir(_HERE) if f.endswith((".c", ".h"))]
+    if not force and os.path.exists(_LIB_PATH):
+        newest = max(os.path.getmtime(s) for s in srcs)
+        if os.path.getmtime(_LIB_PATH) >= newest:
+            return _LIB_PATH
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lp = ctypes.POINTER(ctypes.c_int64)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        L.oracle_qrt.restype = ctypes.c_double
+        L.oracle_qrt.argtypes = [ctypes.c_double]
+        L.oracle_norm.restype = ctypes.c_double
+        L.oracle_norm.argtypes = [dp, ctypes.c_int32, ctypes.c_int32]
+        L.oracle_rhs.restype = None
+        L.oracle_rhs.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, dp, dp, dp, dp]
+        L.oracle_rk_solve_one.restype = ctypes.c_int32
+        L.oracle_rk_solve_one.argtypes = [
+            ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, dp, dp,
+            ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
+        L.oracle_rk_solve_batch.restype = ctypes.c_double
+        L.oracle_rk_solve_batch.argtypes = [
+            ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+            ctypes.c_int32, dp, dp, dp, dp, dp, dp, dp, lp, lp, ip, ctypes.c_int32]
+        if hasattr(L, "oracle_bdf_solve_one"):
+            L.oracle_bdf_solve_one.restype = ctypes.c_int32
+            L.oracle_bdf_solve_one.argtypes = [
+                ctypes.POINTER(_BdfCfg), ctypes.c_int32, ctypes.c_int32, dp, dp,
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
+        if hasattr(L, "oracle_rk_adjoint_one"):
+            L.oracle_rk_adjoint_one.restype = ctypes.c_int32
+            L.oracle_rk_adjoint_one.argtypes = [
+                ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp]
+            L.oracle_rk_frozen_fd_one.restype = ctypes.c_int32
+            L.oracle_rk_frozen_fd_one.argtypes = [
+                ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
+                ctypes.c_double, ctypes.c_double, dp, dp, ctypes.c_double, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def rk_cfg(method=RK45, layout=AS_WRITTEN, pow_mode=POW_QRT, dyn_dim=False,
+           max_attempts=0, tol=1e-6, dt_min=1e-6, dt_max=0.1):
+    return _RkCfg(method, layout, pow_mode, int(dyn_dim), int(max_attempts), tol, dt_min, dt_max)
+
+
+@dataclass
+class Path:
+    status: int
+    t: float
+    y: np.ndarray
+    accepted: int
+    rejected: int
+    traj_t: np.ndarray | None = None
+    traj_y: np.ndarray | None = None
+
+
+def rk_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0) -> Path:
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    dim = y0.shape[0]
+    p = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    y = np.zeros(dim)
+    t = ctypes.c_double()
+    a = ctypes.c_int64()
+    r = ctypes.c_int64()
+    tt = ty = None
+    if traj_cap:
+        tt = np.zeros(traj_cap)
+        ty = np.zeros((traj_cap, dim))
+    st = L.oracle_rk_solve_one(ctypes.byref(cfg), rhs, dim, _dp(p), _dp(sh), t0, t_end,
+                               _dp(y0), _dp(y), ctypes.byref(t), ctypes.byref(a),
+                               ctypes.byref(r), _dp(tt), _dp(ty), traj_cap)
+    if traj_cap:
+        n = min(a.value, traj_cap)
+        tt, ty = tt[:n], ty[:n]
+    return Path(st, t.value, y, a.value, r.value, tt, ty)
+
+
+def rk_solve_batch(cfg, rhs, y0_soa, params_soa, t0, t_end, shared=None, threads=None):
+    """y0_soa: (dim, n); params_soa: (P, n); t0, t_end: (n,).  Returns dict."""
+    L = lib()
+    y0_soa = np.ascontiguousarray(y0_soa, dtype=np.float64)
+    dim, n = y0_soa.shape
+    if params_soa is None or params_soa.size == 0:
+        params_soa = np.zeros((0, n))
+    params_soa = np.ascontiguousarray(params_soa, dtype=np.float64)
+    n_params = params_soa.shape[0]
+    t0 = np.ascontiguousarray(np.broadcast_to(t0, (n,)), dtype=np.float64)
+    t_end = np.ascontiguousarray(np.broadcast_to(t_end, (n,)), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    y = np.zeros((dim, n))
+    t = np.zeros(n)
+    acc = np.zeros(n, dtype=np.int64)
+    rej = np.zeros(n, dtype=np.int64)
+    st = np.zeros(n, dtype=np.int32)
+    threads = threads or os.cpu_count() or 1
+    secs = L.oracle_rk_solve_batch(
+        ctypes.byref(cfg), rhs, dim, n, n_params, _dp(y0_soa),
+        _dp(params_soa) if n_params else None, _dp(sh), _dp(t0), _dp(t_end), _dp(y), _dp(t),
+        acc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        rej.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), threads)
+    return {"y": y, "t": t, "accepted": acc, "rejected": rej, "status": st,
+            "seconds": secs, "threads": threads}
+
+
+def qrt(x: float) -> float:
+    return lib().oracle_qrt(float(x))
+
+
+def norm(x, dyn_dim=False) -> float:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return lib().oracle_norm(_dp(x), x.shape[0], int(dyn_dim))
+
+
+def rhs_eval(rhs, t, y, params=None, shared=None):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    p = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    f = np.zeros_like(y)
+    lib().oracle_rhs(rhs, y.shape[0], t, _dp(y), _dp(p), _dp(sh), _dp(f))
+    return f

@@ -1,0 +1,187 @@
+"""GPU parity of the batched Runge-Kutta engine against the CPU oracle.
+
+Exact mode (FP64_EXACT) must be bit-identical to the oracle's restatement of
+src/ivp/rk.rs:361-423 with the same fourth-root sequence (POW_QRT): final
+states, final times, accepted and rejected counts and statuses.  Every call
+goes through the C ABI (libbacon_gb300.so).
+"""
+import numpy as np
+import pytest
+
+from bacon_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+LAYOUTS = [0, 1, 2]  # as_compiled, as_written, fehlberg
+
+
+def _oracle_batch(O, b, method=0, layout=2, max_attempts=0, pow_mode=None):
+    cfg = O.rk_cfg(method=method, layout=layout, pow_mode=O.POW_QRT if pow_mode is None else pow_mode,
+                   tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, max_attempts=max_attempts)
+    return O.rk_solve_batch(cfg, b.rhs, b.y0, b.params, b.t0, b.t_end)
+
+
+def _gpu_batch(E, b, method=0, layout=2, max_attempts=0, plain=False, precision=0, **kw):
+    return E.rk_solve(b.y0, b.params if b.params.size else None, b.t0, b.t_end, rhs=b.rhs, tol=b.tol,
+                      dt_min=b.dt_min, dt_max=b.dt_max, method=method, layout=layout,
+                      precision=precision, max_attempts=max_attempts, plain=plain, **kw)
+
+
+def _assert_identical(sol, ref):
+    np.testing.assert_array_equal(sol.status, ref["status"])
+    np.testing.assert_array_equal(sol.accepted, ref["accepted"])
+    np.testing.assert_array_equal(sol.rejected, ref["rejected"])
+    np.testing.assert_array_equal(sol.t, ref["t"])
+    np.testing.assert_array_equal(sol.y, ref["y"])
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_vdp_bit_exact(engine, oracle, layout):
+    b = W.van_der_pol(n=1024)
+    cap = 20000 if layout != 2 else 0
+    ref = _oracle_batch(oracle, b, layout=layout, max_attempts=cap)
+    sol = _gpu_batch(engine, b, layout=layout, max_attempts=cap)
+    _assert_identical(sol, ref)
+    if layout == 2:
+        assert sol.code == 0 and (sol.status == 0).all()
+
+
+def test_vdp_config_full_4096(engine, oracle):
+    """The 4096-system Van der Pol workload (t in [0, 10], tol 1e-6)."""
+    b = W.van_der_pol()
+    ref = _oracle_batch(oracle, b, layout=2)
+    sol = _gpu_batch(engine, b, layout=2)
+    _assert_identical(sol, ref)
+
+
+def test_lorenz_subset_bit_exact(engine, oracle):
+    b = W.lorenz(n=1 << 20).subset(np.arange(0, 1 << 20, 512))  # 2048 systems, T ~ U[1, 20]
+    ref = _oracle_batch(oracle, b, layout=2)
+    sol = _gpu_batch(engine, b, layout=2)
+    _assert_identical(sol, ref)
+
+
+def test_lotka_volterra_bit_exact(engine, oracle):
+    b = W.lotka_volterra(n=2048)
+    ref = _oracle_batch(oracle, b, layout=2)
+    sol = _gpu_batch(engine, b, layout=2)
+    _assert_identical(sol, ref)
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_rk23_bit_exact(engine, oracle, layout):
+    b = W.van_der_pol(n=512, seed=11)
+    cap = 20000
+    ref = _oracle_batch(oracle, b, method=1, layout=layout, max_attempts=cap)
+    sol = _gpu_batch(engine, b, method=1, layout=layout, max_attempts=cap)
+    _assert_identical(sol, ref)
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_plain_baseline_matches(engine, oracle, layout):
+    b = W.van_der_pol(n=512, seed=4)
+    cap = 5000
+    ref = _oracle_batch(oracle, b, layout=layout, max_attempts=cap)
+    sol = _gpu_batch(engine, b, layout=layout, max_attempts=cap, plain=True)
+    _assert_identical(sol, ref)
+
+
+def test_status_codes(engine, oracle):
+    """Per-system failures: MinimumTimeDeltaExceeded, MaxAttemptsExceeded,
+    and end <= start (TimeEndOOB) each retire only their own system."""
+    b = W.van_der_pol(n=64, seed=3)
+    b.t_end = b.t_end.copy()
+    b.t_end[5] = -1.0            # end before start
+    b.t_end[9] = 0.0             # end == start
+    b.y0 = b.y0.copy()
+    b.y0[0, 7] = np.nan          # NaN error never accepts: attempt cap
+    b.params = b.params.copy()
+    b.params[0, 11] = 1e6        # stiff: dt collapses below dt_min
+    ref = _oracle_batch(oracle, b, layout=2, max_attempts=3000)
+    sol = _gpu_batch(engine, b, layout=2, max_attempts=3000)
+    _assert_identical(sol, ref)
+    assert sol.status[5] == 5 and sol.status[9] == 5
+    assert sol.status[7] == 13
+    assert sol.status[11] == 8
+    assert sol.code == 5  # lowest failing index is system 5
+    ok = np.ones(64, bool)
+    ok[[5, 7, 9, 11]] = False
+    assert (sol.status[ok] == 0).all()
+
+
+def test_trajectory_matches_oracle_path(engine, oracle):
+    b = W.van_der_pol(n=8, seed=9)
+    cap = 400
+    sol = _gpu_batch(engine, b, layout=2, traj_cap=cap)
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+    for i in range(b.n):
+        p = oracle.rk_solve_one(cfg, b.rhs, b.y0[:, i], 0.0, 10.0, params=b.params[:, i], traj_cap=cap)
+        k = min(p.accepted, cap)
+        assert int(sol.accepted[i]) == p.accepted
+        np.testing.assert_array_equal(sol.traj_t[i, :k], p.traj_t[:k])
+        np.testing.assert_array_equal(sol.traj_y[i, :k], p.traj_y[:k])
+
+
+def test_device_resident_path_matches_host(engine):
+    import torch
+    b = W.lorenz(n=4096, seed=21)
+    host = _gpu_batch(engine, b, layout=2)
+    dev = torch.device("cuda")
+    sol = engine.rk_solve(torch.from_numpy(b.y0).to(dev), torch.from_numpy(b.params).to(dev),
+                          torch.from_numpy(b.t0).to(dev), torch.from_numpy(b.t_end).to(dev), rhs=b.rhs,
+                          tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
+    np.testing.assert_array_equal(sol.y.cpu().numpy(), host.y)
+    np.testing.assert_array_equal(sol.accepted.cpu().numpy(), host.accepted)
+
+
+def test_graph_replay_is_repeatable(engine):
+    b = W.van_der_pol(n=2048, seed=5)
+    out = engine.alloc_outputs(2, b.n, device=False)
+    first = _gpu_batch(engine, b, layout=2, out=out)
+    y1 = first.y.copy()
+    second = _gpu_batch(engine, b, layout=2, out=out)
+    np.testing.assert_array_equal(second.y, y1)
+
+
+def test_fma_mode_close_to_exact(engine):
+    """Contracted arithmetic changes rounding only: VdP is not chaotic, so
+    final states stay within 1e-9 relative."""
+    b = W.van_der_pol(n=2048, seed=8)
+    ex = _gpu_batch(engine, b, layout=2, precision=0)
+    fm = _gpu_batch(engine, b, layout=2, precision=1)
+    assert (fm.status == 0).all()
+    rel = np.abs(fm.y - ex.y).max(axis=0) / np.maximum(np.abs(ex.y).max(axis=0), 1e-300)
+    assert rel.max() <= 1e-9
+    assert np.mean(fm.accepted == ex.accepted) >= 0.99
+
+
+def test_reference_libm_pow_statistics(engine, oracle):
+    """Against the oracle using the platform pow() (what the Rust reference
+    calls): identical accepted counts on >= 99% of systems and final states
+    within 1e-9 relative on the Van der Pol workload."""
+    b = W.van_der_pol()
+    ref = _oracle_batch(oracle, b, layout=2, pow_mode=oracle.POW_LIBM)
+    sol = _gpu_batch(engine, b, layout=2)
+    assert np.mean(sol.accepted == ref["accepted"]) >= 0.99
+    rel = np.abs(sol.y - ref["y"]).max(axis=0) / np.abs(ref["y"]).max(axis=0)
+    assert np.mean(rel <= 1e-9) >= 0.99
+
+
+@pytest.mark.parametrize("kind", ["rk45", "rk23"])
+def test_reference_unit_tests_quadratic_and_sine(engine, kind):
+    """src/ivp/rk.rs:682-758 through the builder mirror, every layout."""
+    from bacon_gb300.ivp import Rhs, RungeKutta23, RungeKutta45
+    cls = RungeKutta45 if kind == "rk45" else RungeKutta23
+    for layout in LAYOUTS:
+        path = (cls.new(1).with_minimum_dt(0.0001).with_maximum_dt(0.1).with_initial_time(0.0)
+                .with_ending_time(10.0).with_tolerance(1e-5).with_initial_conditions_slice([1.0])
+                .with_derivative(Rhs.QUADRATIC).solve((), layout=layout).collect_vec())
+        assert len(path) > 0
+        for t, y in path:
+            assert abs(y[0] - (1.0 - t * t)) <= 0.0001
+        path = (cls.new(1).with_minimum_dt(0.001).with_maximum_dt(0.01).with_tolerance(0.0001)
+                .with_initial_time(0.0).with_ending_time(10.0).with_initial_conditions_slice([0.0])
+                .with_derivative(Rhs.SINE).solve((), layout=layout).collect_vec())
+        assert len(path) > 0
+        for t, y in path:
+            assert abs(y[0] - np.sin(t)) <= 0.01
