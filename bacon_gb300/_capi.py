@@ -31,6 +31,7 @@ STATUS_NAMES = {
     14: "CudaError",
     15: "InvalidArgument",
     16: "Unsupported",
+    17: "CapacityExceeded",
 }
 
 DP = ctypes.POINTER(ctypes.c_double)
@@ -67,7 +68,7 @@ class RkOptions(ctypes.Structure):
         ("block", ctypes.c_int32),
         ("blocks_per_sm", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("schedule", ctypes.c_int32),
     ]
 
 
@@ -85,6 +86,17 @@ class RkResult(ctypes.Structure):
     ]
 
 
+class Adjoint(ctypes.Structure):
+    _fields_ = [
+        ("target", ctypes.c_void_p),
+        ("loss", ctypes.c_void_p),
+        ("dl_dy0", ctypes.c_void_p),
+        ("dl_dp", ctypes.c_void_p),
+        ("checkpoint_every", ctypes.c_int32),
+        ("max_steps", ctypes.c_int32),
+    ]
+
+
 # Every symbol include/bacon_gb300.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 SIGNATURES = {
@@ -92,11 +104,16 @@ SIGNATURES = {
     "bacon_ctx_destroy": (ctypes.c_int, [_VP]),
     "bacon_last_error": (ctypes.c_char_p, []),
     "bacon_ctx_kernel_launches": (ctypes.c_int64, [_VP]),
+    "bacon_ctx_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "bacon_ctx_last_kernel_ms": (ctypes.c_int, [_VP, DP]),
     "bacon_rk_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                       ctypes.POINTER(RkResult)]),
     "bacon_rk_solve_plain": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                             ctypes.POINTER(RkResult)]),
     "bacon_rk_validate": (ctypes.c_int, [ctypes.POINTER(Problem)]),
+    "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                              ctypes.POINTER(RkResult), ctypes.POINTER(Adjoint)]),
+    "bacon_ctx_last_reverse_ms": (ctypes.c_int, [_VP, DP]),
     "bacon_builder_new": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),
     "bacon_builder_new_dyn": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),
     "bacon_builder_free": (None, [_VP]),

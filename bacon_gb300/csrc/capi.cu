@@ -11,9 +11,10 @@
 #include <unordered_map>
 #include <vector>
 
+#include "order.h"
 #include "plain.h"
 #include "registry.h"
-#include "rk_kernel.cuh"
+#include "rk_adjoint.cuh"
 
 namespace bacon {
 double measure_fp64_fma_gflops(cudaStream_t stream, int num_sms);
@@ -105,12 +106,19 @@ struct bacon_ctx {
   std::vector<bacon::RkEntry> kernels;
   DevBuf in_y0, in_params, in_t0, in_tend, out_y, out_t, out_acc, out_rej, out_st, out_tt, out_ty;
   DevBuf pl_y, pl_K, pl_t, pl_dt, pl_end, pl_att, pl_acc, pl_rej, pl_st;
+  DevBuf ord, ord_scratch;  // longest-first work order and its sort scratch
   struct Graph {
     cudaGraphExec_t exec = nullptr;
   };
   std::unordered_map<uint64_t, Graph> graphs;
   std::unordered_map<uint64_t, std::pair<int, int>> tuned;
   int64_t launches = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last main kernel
+  bool ev_valid = false;
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the last adjoint reverse kernel
+  bool rev_valid = false;
+  std::vector<bacon::AdjEntry> adjoint_kernels;
+  DevBuf adj_dt, adj_ck, adj_tgt, adj_loss, adj_gy, adj_gp;
 };
 
 extern "C" {
@@ -135,6 +143,12 @@ int bacon_ctx_create(int device, bacon_ctx** out) {
     return fail(BACON_CUDA_ERROR, std::string("bacon_ctx_create: ") + cudaGetErrorString(e));
   }
   c->kernels = bacon::all_rk_kernels();
+  c->adjoint_kernels = bacon::all_adjoint_kernels();
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess) {
+    bacon_ctx_destroy(c);
+    return fail(BACON_CUDA_ERROR, "bacon_ctx_create: event creation failed");
+  }
   *out = c;
   return BACON_OK;
 }
@@ -147,16 +161,46 @@ int bacon_ctx_destroy(bacon_ctx* c) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   for (DevBuf* b : {&c->in_y0, &c->in_params, &c->in_t0, &c->in_tend, &c->out_y, &c->out_t,
                     &c->out_acc, &c->out_rej, &c->out_st, &c->out_tt, &c->out_ty, &c->pl_y, &c->pl_K,
-                    &c->pl_t, &c->pl_dt, &c->pl_end, &c->pl_att, &c->pl_acc, &c->pl_rej, &c->pl_st})
+                    &c->pl_t, &c->pl_dt, &c->pl_end, &c->pl_att, &c->pl_acc, &c->pl_rej, &c->pl_st,
+                    &c->ord, &c->ord_scratch, &c->adj_dt, &c->adj_ck, &c->adj_tgt, &c->adj_loss,
+                    &c->adj_gy, &c->adj_gp})
     b->release();
+  if (c->ev2) cudaEventDestroy(c->ev2);
+  if (c->ev3) cudaEventDestroy(c->ev3);
   if (c->d_ctl) cudaFree(c->d_ctl);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return BACON_OK;
 }
 
 int64_t bacon_ctx_kernel_launches(const bacon_ctx* c) { return c ? c->launches : 0; }
+
+int bacon_ctx_stream(const bacon_ctx* c, void** stream) {
+  if (!c || !stream) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  *stream = reinterpret_cast<void*>(c->stream);
+  return BACON_OK;
+}
+
+int bacon_ctx_last_reverse_ms(const bacon_ctx* c, double* ms) {
+  if (!c || !ms) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  if (!c->rev_valid) return fail(BACON_INVALID_ARGUMENT, "no adjoint run yet");
+  float f = 0.f;
+  BACON_CUDA(cudaEventElapsedTime(&f, c->ev2, c->ev3));
+  *ms = f;
+  return BACON_OK;
+}
+
+int bacon_ctx_last_kernel_ms(const bacon_ctx* c, double* ms) {
+  if (!c || !ms) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  if (!c->ev_valid) return fail(BACON_INVALID_ARGUMENT, "no timed kernel yet");
+  float f = 0.f;
+  BACON_CUDA(cudaEventElapsedTime(&f, c->ev0, c->ev1));
+  *ms = f;
+  return BACON_OK;
+}
 
 // Builder-equivalent checks on a filled problem (src/ivp/rk.rs:168-256).
 int bacon_rk_validate(const bacon_problem* p) {
@@ -364,6 +408,19 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   a.traj_cap = (o.traj_t ? r->traj_cap : 0);
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
+  a.order = nullptr;
+
+  // Longest-first order when spans differ between systems (or on request).
+  const bool per_system_times = (p->t0 != nullptr) || (p->t_end != nullptr);
+  const bool lpt = (opt->schedule == 2 || (opt->schedule == 0 && per_system_times)) && p->n < (1ll << 32);
+  bacon::OrderArgs oa{};
+  if (lpt) {
+    BACON_CUDA(c->ord.ensure(static_cast<size_t>(p->n) * sizeof(uint32_t)));
+    BACON_CUDA(c->ord_scratch.ensure(sizeof(bacon::OrderScratch)));
+    oa = bacon::OrderArgs{p->n, o.t0, o.t_end, p->t0_scalar, p->t_end_scalar,
+                          c->ord_scratch.as<bacon::OrderScratch>(), c->ord.as<uint32_t>()};
+    a.order = oa.order;
+  }
 
   int block = opt->block > 0 ? opt->block : 128;
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
@@ -388,12 +445,16 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
       if (!is_pinned_or_device(q)) use_graph = false;
   }
 
+  bool capturing = false;
   auto enqueue_all = [&]() -> int {
     int e;
     if (host && (e = enqueue_h2d(c, p, o)) != BACON_OK) return e;
+    if (lpt) BACON_CUDA(bacon::enqueue_lpt_order(oa, c->num_sms, c->stream));
     BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
     BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+    BACON_CUDA(cudaEventRecordWithFlags(c->ev0, c->stream, capturing ? cudaEventRecordExternal : 0));
     BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, 0, c->stream));
+    BACON_CUDA(cudaEventRecordWithFlags(c->ev1, c->stream, capturing ? cudaEventRecordExternal : 0));
     if (host && (e = enqueue_d2h(c, p, r, o)) != BACON_OK) return e;
     BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                c->stream));
@@ -412,7 +473,9 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
     auto it = c->graphs.find(h);
     if (it == c->graphs.end()) {
       BACON_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
       const int e = enqueue_all();
+      capturing = false;
       cudaGraph_t g = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
       if (e != BACON_OK) {
@@ -430,7 +493,8 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   } else {
     if ((rc = enqueue_all()) != BACON_OK) return rc;
   }
-  c->launches += 1;
+  c->launches += lpt ? 5 : 1;
+  c->ev_valid = true;
   BACON_CUDA(cudaStreamSynchronize(c->stream));
   BACON_CUDA(cudaGetLastError());
   return batch_return_code(c, r, host, o);
@@ -526,6 +590,155 @@ extern "C" int bacon_rk_solve_plain(bacon_ctx* c, const bacon_problem* p, const 
   for (size_t i = 0; i < n; ++i)
     if (sp[i] != 0) return fail(sp[i], "system " + std::to_string(i) + " ended with status " + std::to_string(sp[i]));
   return BACON_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Discrete adjoint: recording forward pass, then the reverse kernel.
+extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                      bacon_rk_result* r, bacon_adjoint* adj) {
+  if (!c || !opt || !adj) return fail(BACON_INVALID_ARGUMENT, "NULL context, options or adjoint");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (r->traj_t) return fail(BACON_UNSUPPORTED, "the adjoint records no trajectory");
+  if (opt->precision != BACON_FP64_EXACT) return fail(BACON_UNSUPPORTED, "the adjoint runs in FP64_EXACT");
+  if (opt->layout == BACON_LAYOUT_AS_COMPILED)
+    return fail(BACON_UNSUPPORTED, "the as_compiled matrix reuses stages across attempts: no one-step map");
+  if (p->dyn_dim && p->dim == 4) return fail(BACON_UNSUPPORTED, "dynamic 4-vectors are not compiled");
+  if (p->n > 0 && (!adj->target || !adj->loss || !adj->dl_dy0 || (p->n_params > 0 && !adj->dl_dp)))
+    return fail(BACON_INVALID_ARGUMENT, "adjoint array is NULL");
+  const int every = adj->checkpoint_every > 0 ? adj->checkpoint_every : 32;
+  const int max_steps = adj->max_steps > 0 ? adj->max_steps : 1024;
+  if (every > 32) return fail(BACON_INVALID_ARGUMENT, "checkpoint_every must be in 1..32");
+  const int layout = (opt->method == BACON_RK23) ? 1 : opt->layout;
+  const bacon::RkKey key{opt->method, layout, 0, p->rhs, p->dim};
+  const bacon::AdjEntry* ent = nullptr;
+  for (const auto& e : c->adjoint_kernels)
+    if (e.key == key) ent = &e;
+  if (!ent) return fail(BACON_UNSUPPORTED, "no adjoint kernel for this (method, layout, rhs, dim)");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  const size_t n = static_cast<size_t>(p->n);
+  const int slots = (max_steps + every - 1) / every;
+  BACON_CUDA(c->adj_dt.ensure(n * max_steps * sizeof(double)));
+  BACON_CUDA(c->adj_ck.ensure(n * slots * (p->dim + 1) * sizeof(double)));
+  const double* tgt = adj->target;
+  double *loss = adj->loss, *gy = adj->dl_dy0, *gp = adj->dl_dp;
+  if (host) {
+    BACON_CUDA(c->adj_tgt.ensure(n * p->dim * sizeof(double)));
+    BACON_CUDA(c->adj_loss.ensure(n * sizeof(double)));
+    BACON_CUDA(c->adj_gy.ensure(n * p->dim * sizeof(double)));
+    BACON_CUDA(c->adj_gp.ensure(n * (p->n_params > 0 ? p->n_params : 1) * sizeof(double)));
+    tgt = c->adj_tgt.as<double>();
+    loss = c->adj_loss.as<double>();
+    gy = c->adj_gy.as<double>();
+    gp = c->adj_gp.as<double>();
+  }
+
+  double dt_min = p->dt_min;
+  clamp_dt(dt_min, p->dt_max);
+  bacon::RkArgs a{};
+  a.n = p->n;
+  a.y0 = o.y0;
+  a.params = o.params;
+  a.t0 = o.t0;
+  a.t_end = o.t_end;
+  a.t0_s = p->t0_scalar;
+  a.t_end_s = p->t_end_scalar;
+  a.tol = p->tol;
+  a.dt_min = dt_min;
+  a.dt_max = p->dt_max;
+  a.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  a.y_out = o.y_out;
+  a.t_out = o.t_out;
+  a.accepted = o.acc;
+  a.rejected = o.rej;
+  a.status = o.st;
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+  a.dt_log = c->adj_dt.as<double>();
+  a.ckpt = c->adj_ck.as<double>();
+  a.ckpt_every = every;
+  a.max_steps = max_steps;
+  a.ckpt_slots = slots;
+  const bool per_system_times = (p->t0 != nullptr) || (p->t_end != nullptr);
+  const bool lpt = (opt->schedule == 2 || (opt->schedule == 0 && per_system_times)) && p->n < (1ll << 32);
+  bacon::OrderArgs oa{};
+  if (lpt) {
+    BACON_CUDA(c->ord.ensure(n * sizeof(uint32_t)));
+    BACON_CUDA(c->ord_scratch.ensure(sizeof(bacon::OrderScratch)));
+    oa = bacon::OrderArgs{p->n, o.t0, o.t_end, p->t0_scalar, p->t_end_scalar,
+                          c->ord_scratch.as<bacon::OrderScratch>(), c->ord.as<uint32_t>()};
+    a.order = oa.order;
+  }
+  bacon::AdjArgs b{};
+  b.n = p->n;
+  b.params = o.params;
+  b.y_final = o.y_out;
+  b.accepted = o.acc;
+  b.status = o.st;
+  b.dt_log = a.dt_log;
+  b.ckpt = a.ckpt;
+  b.target = tgt;
+  b.loss = loss;
+  b.dl_dy0 = gy;
+  b.dl_dp = gp;
+  b.max_steps = max_steps;
+  b.ckpt_slots = slots;
+  b.ckpt_every = every;
+  b.queue = c->d_ctl + 3;
+
+  const int block = opt->block > 0 ? opt->block : 128;
+  if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
+  int fwd_bps = 0, rev_bps = 0;
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fwd_bps, ent->fwd, block, 0));
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rev_bps, ent->rev, 128, 0));
+  if (fwd_bps < 1 || rev_bps < 1) return fail(BACON_CUDA_ERROR, "adjoint kernels cannot be resident");
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 1;
+  if (bps > fwd_bps) bps = fwd_bps;
+  const long long need = (p->n + block - 1) / block;
+  long long fgrid = static_cast<long long>(c->num_sms) * bps;
+  if (fgrid > need) fgrid = need;
+  long long rgrid = static_cast<long long>(c->num_sms) * (rev_bps < 2 ? rev_bps : 2);
+  const long long rneed = (p->n + 127) / 128;
+  if (rgrid > rneed) rgrid = rneed;
+
+  if (host) {
+    if ((rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+    BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(tgt), adj->target, n * p->dim * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+  }
+  if (lpt) BACON_CUDA(bacon::enqueue_lpt_order(oa, c->num_sms, c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 3, 0, sizeof(unsigned long long), c->stream));
+  void* fargs[] = {&a};
+  void* rargs[] = {&b};
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(ent->fwd, dim3(static_cast<unsigned>(fgrid)), dim3(block), fargs, 0, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev2, c->stream));
+  BACON_CUDA(cudaLaunchKernel(ent->rev, dim3(static_cast<unsigned>(rgrid)), dim3(128), rargs, 0, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev3, c->stream));
+  if (host) {
+    if ((rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+    BACON_CUDA(cudaMemcpyAsync(adj->loss, loss, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(adj->dl_dy0, gy, n * p->dim * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (p->n_params > 0)
+      BACON_CUDA(cudaMemcpyAsync(adj->dl_dp, gp, n * p->n_params * sizeof(double), cudaMemcpyDeviceToHost,
+                                 c->stream));
+  }
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+  c->launches += lpt ? 6 : 2;
+  c->ev_valid = true;
+  c->rev_valid = true;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  return batch_return_code(c, r, host, o);
 }
 
 // ---------------------------------------------------------------------------

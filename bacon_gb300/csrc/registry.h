@@ -23,11 +23,24 @@ struct RkEntry {
   const void* fn;  // __global__ void(RkArgs)
 };
 
+struct AdjEntry {
+  RkKey key;
+  const void* fwd;  // recording forward kernel, __global__ void(RkArgs)
+  const void* rev;  // reverse kernel, __global__ void(AdjArgs)
+};
+
+template <class T>
+struct TypeTag {
+  using type = T;
+};
+
 void register_rk45_exact_l0(std::vector<RkEntry>& v);
 void register_rk45_exact_l1(std::vector<RkEntry>& v);
 void register_rk45_exact_l2(std::vector<RkEntry>& v);
 void register_rk45_fma(std::vector<RkEntry>& v);
 void register_rk23(std::vector<RkEntry>& v);
+void register_adjoint_rk45(std::vector<AdjEntry>& v);
+void register_adjoint_rk23(std::vector<AdjEntry>& v);
 
 inline std::vector<RkEntry> all_rk_kernels() {
   std::vector<RkEntry> v;
@@ -36,6 +49,13 @@ inline std::vector<RkEntry> all_rk_kernels() {
   register_rk45_exact_l2(v);
   register_rk45_fma(v);
   register_rk23(v);
+  return v;
+}
+
+inline std::vector<AdjEntry> all_adjoint_kernels() {
+  std::vector<AdjEntry> v;
+  register_adjoint_rk45(v);
+  register_adjoint_rk23(v);
   return v;
 }
 

@@ -114,6 +114,88 @@ struct RhsLotka {  // a x - b x y, c x y - d y
   }
 };
 
+// ---- vector-Jacobian products for the discrete adjoint --------------------
+// ubar = J_f(y)^T v and pbar = (df/dp)(y)^T v.  The reference has no
+// gradients; these are evaluated in the same order as the CPU oracle's
+// rhs_vjp (oracle/adjoint_oracle.c) so that the adjoint is bit-reproducible.
+template <class R>
+struct Vjp;
+
+template <int D>
+struct Vjp<RhsExp<D>> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&)[D], const double*, const double (&v)[D],
+                                              double (&ub)[D], double*) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) ub[d] = v[d];
+  }
+};
+
+template <int D>
+struct Vjp<RhsDecay<D>> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&)[D], const double*, const double (&v)[D],
+                                              double (&ub)[D], double*) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) ub[d] = -v[d];
+  }
+};
+
+template <>
+struct Vjp<RhsHarmonic> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&)[2], const double*, const double (&v)[2],
+                                              double (&ub)[2], double*) {
+    ub[0] = -v[1];
+    ub[1] = v[0];
+  }
+};
+
+template <>
+struct Vjp<RhsVdp> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&y)[2], const double* p, const double (&v)[2],
+                                              double (&ub)[2], double* pb) {
+    const double mu = p[0];
+    const double w = Ops::sub(1.0, Ops::mul(y[0], y[0]));
+    ub[0] = Ops::mul(Ops::sub(Ops::mul(Ops::mul(Ops::mul(-2.0, mu), y[0]), y[1]), 1.0), v[1]);
+    ub[1] = Ops::add(v[0], Ops::mul(Ops::mul(mu, w), v[1]));
+    pb[0] = Ops::mul(Ops::mul(w, y[1]), v[1]);
+  }
+};
+
+template <>
+struct Vjp<RhsLorenz> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&y)[3], const double* p, const double (&v)[3],
+                                              double (&ub)[3], double* pb) {
+    const double s = p[0], r = p[1], b = p[2];
+    ub[0] = Ops::add(Ops::add(Ops::mul(-s, v[0]), Ops::mul(Ops::sub(r, y[2]), v[1])), Ops::mul(y[1], v[2]));
+    ub[1] = Ops::add(Ops::sub(Ops::mul(s, v[0]), v[1]), Ops::mul(y[0], v[2]));
+    ub[2] = Ops::sub(Ops::mul(-y[0], v[1]), Ops::mul(b, v[2]));
+    pb[0] = Ops::mul(Ops::sub(y[1], y[0]), v[0]);
+    pb[1] = Ops::mul(y[0], v[1]);
+    pb[2] = -Ops::mul(y[2], v[2]);
+  }
+};
+
+template <>
+struct Vjp<RhsLotka> {
+  template <class Ops>
+  __device__ __forceinline__ static void eval(const double (&y)[2], const double* p, const double (&v)[2],
+                                              double (&ub)[2], double* pb) {
+    const double a = p[0], b = p[1], c = p[2], dd = p[3];
+    const double x = y[0], w = y[1];
+    ub[0] = Ops::add(Ops::mul(Ops::sub(a, Ops::mul(b, w)), v[0]), Ops::mul(Ops::mul(c, w), v[1]));
+    ub[1] = Ops::add(Ops::mul(-Ops::mul(b, x), v[0]), Ops::mul(Ops::sub(Ops::mul(c, x), dd), v[1]));
+    const double xw = Ops::mul(x, w);
+    pb[0] = Ops::mul(x, v[0]);
+    pb[1] = -Ops::mul(xw, v[0]);
+    pb[2] = Ops::mul(xw, v[1]);
+    pb[3] = -Ops::mul(w, v[1]);
+  }
+};
+
 struct RhsRobertson {  // k1, k2, k3 kinetics
   static constexpr int DIM = 3, NP = 3;
   static constexpr bool kUsesT = false;

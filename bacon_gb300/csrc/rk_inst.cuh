@@ -7,11 +7,6 @@
 
 namespace bacon {
 
-template <class T>
-struct TypeTag {
-  using type = T;
-};
-
 template <class Lit, int L, class Ops>
 void register_rk_set(std::vector<RkEntry>& v, int method, int prec) {
   auto add = [&](auto tag, int rhs_id) {

@@ -27,6 +27,7 @@ enum : int32_t {
   kStMaxIter = 9,
   kStSingular = 10,
   kStMaxAttempts = 13,
+  kStCapacity = 17,
 };
 
 struct RkArgs {
@@ -48,6 +49,15 @@ struct RkArgs {
   int32_t traj_cap;
   unsigned long long* queue;       // work counter, zero at launch
   unsigned long long* first_fail;  // lowest failing index, ~0 at launch
+  const uint32_t* order;           // work order (a permutation of [0, n)) or null
+  // Adjoint recording (kRecord kernels only): per accepted step k the dt it
+  // used, dt_log[i*max_steps + k]; every ckpt_every accepted steps the
+  // (t, y) it started from, ckpt[(i*ckpt_slots + k/ckpt_every)*(D+1) + {0, 1+d}].
+  double* dt_log;
+  double* ckpt;
+  int32_t ckpt_every;
+  int32_t max_steps;
+  int32_t ckpt_slots;
 };
 
 template <int I, int N, class F>
@@ -82,7 +92,7 @@ __device__ __forceinline__ void poison_components(double (&v)[D], uint32_t mask)
   }
 }
 
-template <class Tab, class Rhs, class Ops>
+template <class Tab, class Rhs, class Ops, bool kRecord = false>
 __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
   constexpr int D = Rhs::DIM;
   constexpr int S = Tab::S;
@@ -113,7 +123,7 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
       if (need) {
         const int64_t cand = static_cast<int64_t>(base) + __popc(need_mask & lt_mask);
         if (cand < n) {
-          idx = cand;
+          idx = a.order ? static_cast<int64_t>(a.order[cand]) : cand;
           have = true;
           t = a.t0 ? a.t0[idx] : a.t0_s;
           end = a.t_end ? a.t_end[idx] : a.t_end_s;
@@ -151,6 +161,8 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
     if (fin < 0) {
       ++attempts;
       if (Ops::add(t, dt) >= end) dt = Ops::sub(end, t);  // rk.rs:366-368
+      const double dt_used = dt;
+      (void)dt_used;
 
       // Stages (rk.rs:370-384): scratch = y + sum_j M[i][j] K_j; K_i = f(.) * dt.
       static_for<0, S>([&](auto ic) {
@@ -231,7 +243,18 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
 
       if (dt < dt_min && (ok ? tn : t) < end) {
         fin = kStMinDt;  // the accepted state of this attempt is never yielded
+      } else if (kRecord && ok && acc >= a.max_steps) {
+        fin = kStCapacity;  // the step log is full
       } else if (ok) {
+        if constexpr (kRecord) {
+          a.dt_log[idx * a.max_steps + acc] = dt_used;
+          if (acc % a.ckpt_every == 0) {
+            double* c = a.ckpt + (idx * a.ckpt_slots + acc / a.ckpt_every) * (D + 1);
+            c[0] = t;
+#pragma unroll
+            for (int d = 0; d < D; ++d) c[1 + d] = y[d];
+          }
+        }
         if (a.traj_t != nullptr && acc < a.traj_cap) {
           const int64_t slot = idx * a.traj_cap + acc;
           a.traj_t[slot] = tn;

@@ -60,6 +60,26 @@ class Context:
     def kernel_launches(self) -> int:
         return int(self._lib.bacon_ctx_kernel_launches(self.handle))
 
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        s = ctypes.c_void_p()
+        check(self._lib.bacon_ctx_stream(self.handle, ctypes.byref(s)))
+        return int(s.value or 0)
+
+    def last_kernel_ms(self) -> float:
+        """Device time of the last solve's main kernel (CUDA events on the
+        context's stream)."""
+        ms = ctypes.c_double()
+        check(self._lib.bacon_ctx_last_kernel_ms(self.handle, ctypes.byref(ms)))
+        return ms.value
+
+    def last_reverse_ms(self) -> float:
+        """Device time of the last adjoint's reverse kernel."""
+        ms = ctypes.c_double()
+        check(self._lib.bacon_ctx_last_reverse_ms(self.handle, ctypes.byref(ms)))
+        return ms.value
+
     def fp64_peak_gflops(self) -> float:
         g = ctypes.c_double()
         check(self._lib.bacon_measure_fp64_peak(self.handle, ctypes.byref(g)))
@@ -127,12 +147,13 @@ def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False)
 
 
 def rk_options(method=RK45, layout=FEHLBERG, precision=FP64_EXACT, memory=MEM_HOST, max_attempts=0,
-               block=0, blocks_per_sm=0, use_graph=True):
+               block=0, blocks_per_sm=0, use_graph=True, schedule=0):
     o = _capi.RkOptions()
     o.method, o.layout, o.precision, o.memory = method, layout, precision, memory
     o.max_attempts = int(max_attempts)
     o.block, o.blocks_per_sm = int(block), int(blocks_per_sm)
     o.use_graph = int(bool(use_graph))
+    o.schedule = int(schedule)
     return o
 
 
@@ -179,7 +200,7 @@ def make_result(out, traj_cap=0):
 def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
              precision=FP64_EXACT, max_attempts=0, traj_cap=0, ctx: Context | None = None,
              plain=False, block=0, blocks_per_sm=0, use_graph=True, dyn_dim=False, out=None,
-             raise_on_error=False) -> Solution:
+             raise_on_error=False, schedule=0) -> Solution:
     """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors."""
     ctx = ctx or default_context()
     device = _is_device(y0)
@@ -194,7 +215,7 @@ def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, la
     dim, n = int(y0.shape[0]), int(y0.shape[1])
     prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim)
     opts = rk_options(method, layout, precision, MEM_DEVICE if device else MEM_HOST, max_attempts,
-                      block, blocks_per_sm, use_graph)
+                      block, blocks_per_sm, use_graph, schedule)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
     res = make_result(out, traj_cap)
@@ -205,3 +226,60 @@ def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, la
         raise IVPError(code, _capi.last_error())
     return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code),
                     out.get("traj_t"), out.get("traj_y"))
+
+
+@dataclass
+class AdjointSolution:
+    """Forward outcome plus the loss and its gradients per system."""
+    forward: Solution
+    loss: Any      # (n,)
+    dl_dy0: Any    # (dim, n)
+    dl_dp: Any     # (n_params, n) or None
+    code: int
+
+
+def rk_solve_adjoint(y0, params, t0, t_end, target, *, rhs, tol, dt_min, dt_max, method=RK45,
+                     layout=FEHLBERG, max_attempts=0, checkpoint_every=32, max_steps=1024,
+                     ctx: Context | None = None, block=0, blocks_per_sm=0, out=None, grads=None,
+                     schedule=0, raise_on_error=False) -> AdjointSolution:
+    """Batched solve_ivp_adjoint: loss_i = ||y_i(T) - target_i||^2 and its
+    gradient with respect to y0_i and params_i (discrete adjoint, checkpoints
+    every ``checkpoint_every`` accepted steps)."""
+    ctx = ctx or default_context()
+    device = _is_device(y0)
+    if not device:
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        target = np.ascontiguousarray(target, dtype=np.float64)
+        if params is not None:
+            params = np.ascontiguousarray(params, dtype=np.float64)
+        if not np.isscalar(t0):
+            t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        if not np.isscalar(t_end):
+            t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    n_params = 0 if params is None else int(params.shape[0])
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs)
+    opts = rk_options(method, layout, FP64_EXACT, MEM_DEVICE if device else MEM_HOST, max_attempts,
+                      block, blocks_per_sm, False, schedule)
+    if out is None:
+        out = alloc_outputs(dim, n, device)
+    if grads is None:
+        if device:
+            import torch
+            mk = lambda *s: torch.empty(s, dtype=torch.float64, device=y0.device)  # noqa: E731
+        else:
+            mk = lambda *s: np.empty(s, dtype=np.float64)  # noqa: E731
+        grads = dict(loss=mk(n), dl_dy0=mk(dim, n), dl_dp=mk(max(n_params, 1), n))
+    res = make_result(out)
+    adj = _capi.Adjoint()
+    adj.target = _ptr(target)
+    adj.loss, adj.dl_dy0 = _ptr(grads["loss"]), _ptr(grads["dl_dy0"])
+    adj.dl_dp = _ptr(grads["dl_dp"]) if n_params else None
+    adj.checkpoint_every, adj.max_steps = int(checkpoint_every), int(max_steps)
+    code = _capi.load().bacon_rk_solve_adjoint(ctx.handle, ctypes.byref(prob), ctypes.byref(opts),
+                                               ctypes.byref(res), ctypes.byref(adj))
+    if code in (14, 15, 16) or (raise_on_error and code != 0):
+        raise IVPError(code, _capi.last_error())
+    fwd = Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code))
+    return AdjointSolution(fwd, grads["loss"], grads["dl_dy0"], grads["dl_dp"] if n_params else None,
+                           int(code))

@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Benchmark: batched RK45 solves/s of the GB300 engine.
+
+One step = one batched solve of 1,048,576 independent Lorenz-63 systems
+(sigma ~ U[9,11], rho ~ U[20,30], beta ~ U[2.4,2.9], y0 ~ N(0, 5^2 I),
+end times T ~ U[1,20], tol 1e-6) with the RKF45 engine in FP64 arithmetic that
+is bit-identical to the CPU restatement of the reference (tableau variant
+"fehlberg": the reference's as-compiled matrix does not integrate these
+systems).  Inputs are generated from fixed seeds.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bacon|reference]
+
+Under torchrun every rank solves its own batch of the same size (weak
+scaling, no collective on the data path); the reported value is the total
+over ranks divided by the slowest rank's time.  ``--impl reference`` times
+the CPU restatement of the reference solver on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched RK45 solves/s & adjoint grads/s @rtol 1e-6 vs plain GPU RK45 & CPU"
+UNIT = "solves/s"
+L2_FLUSH_BYTES = 256 << 20   # larger than the 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="bacon", choices=["bacon", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20, help="systems per GPU")
+    ap.add_argument("--cpu-sample", type=int, default=16384, help="systems in the CPU sample")
+    ap.add_argument("--skip-extras", action="store_true", help="skip plain/FMA/CPU side measurements")
+    return ap.parse_args()
+
+
+def workload(n, rank):
+    from bacon_gb300 import workloads as W
+    return W.lorenz(n=n, seed=2 + rank)
+
+
+def config(args, b):
+    return {"workload": "lorenz63", "n_systems_per_gpu": b.n, "dim": 3, "tol": b.tol,
+            "dt_min": b.dt_min, "dt_max": b.dt_max, "t0": 0.0, "t_end": "U[1,20] per system",
+            "method": "RKF45", "tableau": "fehlberg", "precision": "fp64_exact",
+            "parity": "bit-identical to the CPU restatement (tests/test_rk_gpu.py)",
+            "l2": "256 MiB device write before every timed step (inputs ~100 MB fit in L2)",
+            "parallelism": f"replicas x{args.gpus} (independent batches, no collective)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.lines:
+            return {"unavailable": "nvidia-smi produced no samples"}
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"unavailable": "unparsable nvidia-smi output"}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference solver on the host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    b = workload(args.n, 0)
+    rng = np.random.default_rng(123)
+    idx = np.sort(rng.choice(b.n, size=min(args.cpu_sample, b.n), replace=False))
+    s = b.subset(idx)
+    cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_LIBM, tol=s.tol, dt_min=s.dt_min, dt_max=s.dt_max)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.rk_solve_batch(cfg, s.rhs, s.y0[:, :256], s.params[:, :256], s.t0[:256], s.t_end[:256], threads=threads)
+    secs = []
+    for _ in range(args.steps):
+        r = O.rk_solve_batch(cfg, s.rhs, s.y0, s.params, s.t0, s.t_end, threads=threads)
+        secs.append(r["seconds"])
+    value = s.n * len(secs) / sum(secs)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded numpy)", "config": config(args, b),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{s.n} of the {b.n} Lorenz systems per step (seeded subset); "
+                                       "C restatement of src/ivp/rk.rs with the platform pow()"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from bacon_gb300 import engine as E
+    from bacon_gb300 import roofline as R
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    ctx = E.Context(local)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    b = workload(args.n, rank)
+    fp64_peak = ctx.fp64_peak_gflops()
+
+    y0 = torch.from_numpy(b.y0).to(dev)
+    prm = torch.from_numpy(b.params).to(dev)
+    t0 = torch.from_numpy(b.t0).to(dev)
+    te = torch.from_numpy(b.t_end).to(dev)
+    out = E.alloc_outputs(3, b.n, device=True)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def solve(precision=E.FP64_EXACT, dst=None):
+        return E.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=E.FEHLBERG, precision=precision, out=dst or out, ctx=ctx,
+                          raise_on_error=True)
+
+    for _ in range(max(args.warmup, 0)):
+        solve()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    step_ms, kern_ms = [], []
+    launches0 = ctx.kernel_launches
+    barrier()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            solve()
+            e1.record(ext)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(ctx.last_kernel_ms())
+        barrier()
+    wall = time.perf_counter() - wall0
+    launches = ctx.kernel_launches - launches0
+
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = b.n * world * args.steps / (total_ms * 1e-3)
+
+    acc = out["accepted"].cpu().numpy().astype(np.int64)
+    rej = out["rejected"].cpu().numpy().astype(np.int64)
+    status = out["status"].cpu().numpy()
+    attempts = int(acc.sum() + rej.sum())
+    flops = R.rk_flops(0, b.rhs, 3, attempts, int(acc.sum()))
+    kavg = sum(kern_ms) / len(kern_ms)
+    achieved = flops / (kavg * 1e-3) / 1e12
+    peak = fp64_peak / 1e3
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "rk_persistent_lorenz_1m.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    # ---- end to end: host (pinned) buffers through the C ABI ----
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    hy0, hprm, ht0, hte = pin(b.y0), pin(b.params), pin(b.t0), pin(b.t_end)
+    hout = E.alloc_outputs(3, b.n, device=False, pin=True)
+    h2d = hy0.nbytes + hprm.nbytes + ht0.nbytes + hte.nbytes
+    d2h = sum(hout[k].nbytes for k in ("y", "t", "accepted", "rejected", "status"))
+    E.rk_solve(hy0, hprm, ht0, hte, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+               layout=E.FEHLBERG, out=hout, ctx=ctx, raise_on_error=True)
+    barrier()
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        E.rk_solve(hy0, hprm, ht0, hte, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                   layout=E.FEHLBERG, out=hout, ctx=ctx, raise_on_error=True)
+        e2e_s.append(time.perf_counter() - s0)
+    e2e_total = sum(e2e_s)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = b.n * world * args.steps / e2e_total
+    assert np.array_equal(hout["y"], out["y"].cpu().numpy()), "host and device paths disagree"
+
+    extras = {}
+    if not args.skip_extras:
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        fout = E.alloc_outputs(3, b.n, device=True)
+        s0 = time.perf_counter()
+        solve(E.FP64_FMA, fout)
+        torch.cuda.synchronize()
+        extras["fp64_fma_mode"] = {"value": b.n / (time.perf_counter() - s0), "unit": UNIT,
+                                   "note": "same workload, products and sums contracted (not bit-exact)"}
+        pout = E.alloc_outputs(3, b.n, device=True)
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        E.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                   layout=E.FEHLBERG, out=pout, ctx=ctx, plain=True, raise_on_error=True)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - s0
+        same = bool(torch.equal(pout["y"], out["y"]))
+        extras["plain_gpu_baseline"] = {
+            "value": b.n / plain_s, "unit": UNIT, "identical_results": same,
+            "what": "one launch per attempt, state in HBM, dense tableau, host loop until done"}
+        extras["speedup_vs_plain"] = value / world / (b.n / plain_s)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded numpy, Lorenz-63 batch)", "config": config(args, b),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "measured live (FP64 FMA probe kernel); MEASURED_PEAKS.json has no FP64 entry",
+                         "flops_per_launch": flops, "kernel_ms": kavg,
+                         "work": "194 flops per attempt + 25 per accepted attempt (bacon_gb300/roofline.py)"},
+            "clocks": clocks.summary(), "wall_s_timed_region": wall,
+            "statuses_ok": bool((status == 0).all()), "attempts_per_solve": attempts / b.n}
+    line.update(extras)
+
+    if rank == 0 and world == 1 and not args.skip_extras:
+        from oracle import oracle as O
+        rng = np.random.default_rng(123)
+        idx = np.sort(rng.choice(b.n, size=min(args.cpu_sample, b.n), replace=False))
+        s = b.subset(idx)
+        threads = os.cpu_count() or 1
+        cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_QRT, tol=s.tol, dt_min=s.dt_min, dt_max=s.dt_max)
+        r = O.rk_solve_batch(cfg, s.rhs, s.y0, s.params, s.t0, s.t_end, threads=threads)
+        line["cpu_baseline"] = {
+            "value": s.n / r["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{s.n} of the {b.n} Lorenz systems (seeded subset), all host threads",
+            "sample_bit_identical": bool(np.array_equal(r["y"], out["y"].cpu().numpy()[:, idx])
+                                         and np.array_equal(r["accepted"], acc[idx]))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

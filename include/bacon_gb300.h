@@ -47,7 +47,9 @@ typedef enum {
   BACON_MAX_ATTEMPTS_EXCEEDED = 13,
   BACON_CUDA_ERROR = 14,
   BACON_INVALID_ARGUMENT = 15,
-  BACON_UNSUPPORTED = 16
+  BACON_UNSUPPORTED = 16,
+  /* A system took more accepted steps than the adjoint's step log holds. */
+  BACON_CAPACITY_EXCEEDED = 17
 } bacon_status;
 
 /* ---- right-hand sides --------------------------------------------------- */
@@ -108,6 +110,12 @@ int bacon_ctx_destroy(bacon_ctx* ctx);
 const char* bacon_last_error(void);
 /* Number of kernels the context launched since creation (diagnostics). */
 int64_t bacon_ctx_kernel_launches(const bacon_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events after the engine's. */
+int bacon_ctx_stream(const bacon_ctx* ctx, void** stream);
+/* Device time in milliseconds of the last solve's main integration kernel,
+ * from CUDA events recorded around it on the context's stream. */
+int bacon_ctx_last_kernel_ms(const bacon_ctx* ctx, double* ms);
 
 /* ---- batch description -------------------------------------------------- */
 /* One solve of n independent systems of dimension `dim`.  All arrays are SoA
@@ -142,7 +150,10 @@ typedef struct {
   int32_t block;          /* threads per block, 0 = autotuned */
   int32_t blocks_per_sm;  /* persistent CTAs per SM, 0 = autotuned */
   int32_t use_graph;      /* 1: launch through a cached CUDA graph */
-  int32_t reserved;
+  /* Work order of the persistent kernel: 0 = longest span first when the
+   * systems have per-system start or end times, index order otherwise;
+   * 1 = index order; 2 = longest span first. */
+  int32_t schedule;
 } bacon_rk_options;
 
 /* Outputs, same memory kind as the inputs.  (t_final, y_final) is the last
@@ -177,6 +188,31 @@ int bacon_rk_solve(bacon_ctx* ctx, const bacon_problem* problem,
 int bacon_rk_solve_plain(bacon_ctx* ctx, const bacon_problem* problem,
                          const bacon_rk_options* options,
                          bacon_rk_result* result);
+
+/* ---- discrete adjoint ---------------------------------------------------- */
+/* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with
+ * respect to its initial state and parameters, through the accepted-step
+ * sequence of the forward solve (step sizes held fixed: the gradient of the
+ * discrete map).  The reference has no gradient entry point; this is the
+ * batched `solve_ivp_adjoint`.  The forward pass logs each accepted dt and
+ * checkpoints (t, y) every `checkpoint_every` accepted steps; the backward
+ * pass replays each segment from its checkpoint and sweeps it in reverse.
+ * Same memory kind as the problem.  Tableau layouts AS_WRITTEN / FEHLBERG,
+ * FP64_EXACT only. */
+typedef struct {
+  const double* target;     /* [dim][n] */
+  double* loss;             /* [n] */
+  double* dl_dy0;           /* [dim][n] */
+  double* dl_dp;            /* [n_params][n], NULL when n_params == 0 */
+  int32_t checkpoint_every; /* accepted steps per checkpoint, 1..32; 0 = 32 */
+  int32_t max_steps;        /* accepted steps logged per system; 0 = 1024 */
+} bacon_adjoint;
+
+int bacon_rk_solve_adjoint(bacon_ctx* ctx, const bacon_problem* problem,
+                           const bacon_rk_options* options, bacon_rk_result* result,
+                           bacon_adjoint* adjoint);
+/* Device time in milliseconds of the last adjoint's reverse kernel. */
+int bacon_ctx_last_reverse_ms(const bacon_ctx* ctx, double* ms);
 
 /* Validate a problem the way the reference builder does (rk.rs:168-256):
  * tolerance, dt bounds, start/end order, missing parameters.  No GPU work. */

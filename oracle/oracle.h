@@ -147,14 +147,22 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
                              double* traj_t, double* traj_y, int64_t traj_cap);
 
 /* ---- gradients (no reference counterpart; oracle for the adjoint) ------- */
-/* Discrete adjoint of an accepted-step sequence of the as_written RK45 with
- * QRT controller, loss = sum_d (y_T[d] - target[d])^2.  Fills dL/dy0[dim] and
- * dL/dp[n_params].  Returns the forward status. */
+/* Discrete adjoint of the accepted-step sequence of a forward solve (step
+ * sizes frozen), loss = sum_d (y_T[d] - target[d])^2.  Fills dL/dy0[dim] and
+ * dL/dp[n_params] and the loss.  Returns the forward status (-1 for the
+ * as_compiled reading, which has no one-step map). */
 int32_t oracle_rk_adjoint_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
                               int32_t n_params, const double* p, double t0,
                               double t_end, const double* y0,
                               const double* target, double* loss,
                               double* dl_dy0, double* dl_dp);
+
+/* Forward (tangent-linear) sensitivities of the same loss through the same
+ * frozen step sequence; agrees with the adjoint up to rounding. */
+int32_t oracle_rk_fwdsens_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
+                              int32_t n_params, const double* p, double t0,
+                              double t_end, const double* y0,
+                              const double* target, double* dl_dy0, double* dl_dp);
 
 /* Same loss differentiated by replaying the forward run's accepted dt sequence
  * with perturbed inputs (frozen steps), central differences with step h. */

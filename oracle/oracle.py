@@ -98,6 +98,10 @@ def lib():
             L.oracle_rk_adjoint_one.argtypes = [
                 ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
                 ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp]
+            L.oracle_rk_fwdsens_one.restype = ctypes.c_int32
+            L.oracle_rk_fwdsens_one.argtypes = [
+                ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, dp]
             L.oracle_rk_frozen_fd_one.restype = ctypes.c_int32
             L.oracle_rk_frozen_fd_one.argtypes = [
                 ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
@@ -195,3 +199,41 @@ def rhs_eval(rhs, t, y, params=None, shared=None):
     f = np.zeros_like(y)
     lib().oracle_rhs(rhs, y.shape[0], t, _dp(y), _dp(p), _dp(sh), _dp(f))
     return f
+
+
+def rk_adjoint_one(cfg, rhs, y0, params, t0, t_end, target):
+    """Discrete adjoint (oracle): returns (status, loss, dL/dy0, dL/dp)."""
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    gy = np.zeros(y0.shape[0])
+    gp = np.zeros(p.shape[0])
+    loss = ctypes.c_double()
+    st = L.oracle_rk_adjoint_one(ctypes.byref(cfg), rhs, y0.shape[0], p.shape[0], _dp(p), t0, t_end,
+                                 _dp(y0), _dp(tg), ctypes.byref(loss), _dp(gy), _dp(gp))
+    return st, loss.value, gy, gp
+
+
+def rk_frozen_fd_one(cfg, rhs, y0, params, t0, t_end, target, h=1e-6):
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    gy = np.zeros(y0.shape[0])
+    gp = np.zeros(p.shape[0])
+    st = L.oracle_rk_frozen_fd_one(ctypes.byref(cfg), rhs, y0.shape[0], p.shape[0], _dp(p), t0, t_end,
+                                   _dp(y0), _dp(tg), h, _dp(gy), _dp(gp))
+    return st, gy, gp
+
+
+def rk_fwdsens_one(cfg, rhs, y0, params, t0, t_end, target):
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    gy = np.zeros(y0.shape[0])
+    gp = np.zeros(p.shape[0])
+    st = L.oracle_rk_fwdsens_one(ctypes.byref(cfg), rhs, y0.shape[0], p.shape[0], _dp(p), t0, t_end,
+                                 _dp(y0), _dp(tg), _dp(gy), _dp(gp))
+    return st, gy, gp

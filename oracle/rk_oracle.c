@@ -20,7 +20,6 @@
 #include <string.h>
 #include <time.h>
 
-#define ORC_MAX_STAGES 6
 
 /* ------------------------------------------------------------------------ */
 /* Right-hand sides.  Formulas are written with explicit parentheses; the
@@ -179,15 +178,9 @@ double oracle_norm(const double* x, int32_t n, int32_t dyn_dim) {
 /* ------------------------------------------------------------------------ */
 /* Tableaux, built coefficient by coefficient the way the reference computes
  * them (src/ivp/rk.rs:435-525 and :568-620). */
-typedef struct {
-  int s;
-  double c[ORC_MAX_STAGES];
-  double m[ORC_MAX_STAGES][ORC_MAX_STAGES]; /* matrix as read by row_iter */
-  double b[ORC_MAX_STAGES];
-  double e[ORC_MAX_STAGES];
-} orc_tableau;
+#include "oracle_internal.h"
 
-static void tableau_build(int method, int layout, orc_tableau* tb) {
+void orc_tableau_build(int method, int layout, orc_tableau* tb) {
   double a[ORC_MAX_STAGES][ORC_MAX_STAGES];
   memset(tb, 0, sizeof(*tb));
   memset(a, 0, sizeof(a));
@@ -236,15 +229,15 @@ static void tableau_build(int method, int layout, orc_tableau* tb) {
 }
 
 /* ------------------------------------------------------------------------ */
-#define ORC_MAX_DIM 512
 
-int32_t oracle_rk_solve_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
-                            const double* p, const double* shared, double t0,
-                            double t_end, const double* y0, double* y_out,
-                            double* t_out, int64_t* accepted, int64_t* rejected,
-                            double* traj_t, double* traj_y, int64_t traj_cap) {
+
+int32_t orc_rk_solve_core(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
+                          const double* p, const double* shared, double t0, double t_end,
+                          const double* y0, double* y_out, double* t_out, int64_t* accepted,
+                          int64_t* rejected, double* traj_t, double* traj_y, int64_t traj_cap,
+                          double* dt_log, double* t_log, double* y_log, int64_t log_cap) {
   orc_tableau tb;
-  tableau_build(cfg->method, cfg->layout, &tb);
+  orc_tableau_build(cfg->method, cfg->layout, &tb);
   const int s = tb.s;
   double y[ORC_MAX_DIM], scratch[ORC_MAX_DIM], f[ORC_MAX_DIM];
   double K[ORC_MAX_STAGES][ORC_MAX_DIM];
@@ -293,6 +286,9 @@ int32_t oracle_rk_solve_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
     const double error = oracle_norm(scratch, dim, cfg->dyn_dim) / dt;
 
     const int ok = (error <= tol);
+    const double dt_used = dt, t_prev = t;
+    double y_prev[ORC_MAX_DIM];
+    if (dt_log) memcpy(y_prev, y, sizeof(double) * dim);
     if (ok) {
       t = t + dt;
       for (int j = 0; j < s; ++j)
@@ -310,6 +306,12 @@ int32_t oracle_rk_solve_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
     if (dt < dt_min && t < end) { status = ORC_MINIMUM_TIME_DELTA_EXCEEDED; break; }
 
     if (ok) {
+      if (dt_log && acc < log_cap) {
+        /* the step just accepted started at (t - dt_used, y_prev) */
+        dt_log[acc] = dt_used;
+        t_log[acc] = t_prev;
+        memcpy(y_log + (size_t)acc * dim, y_prev, sizeof(double) * dim);
+      }
       if (traj_t && acc < traj_cap) {
         traj_t[acc] = t;
         memcpy(traj_y + (size_t)acc * dim, y, sizeof(double) * dim);
@@ -325,6 +327,15 @@ int32_t oracle_rk_solve_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
   *accepted = acc;
   *rejected = rej;
   return status;
+}
+
+int32_t oracle_rk_solve_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
+                            const double* p, const double* shared, double t0,
+                            double t_end, const double* y0, double* y_out,
+                            double* t_out, int64_t* accepted, int64_t* rejected,
+                            double* traj_t, double* traj_y, int64_t traj_cap) {
+  return orc_rk_solve_core(cfg, rhs, dim, p, shared, t0, t_end, y0, y_out, t_out, accepted,
+                           rejected, traj_t, traj_y, traj_cap, NULL, NULL, NULL, 0);
 }
 
 /* ------------------------------------------------------------------------ */
