@@ -83,9 +83,11 @@ __device__ __forceinline__ double qrt(double x) {
     x = __dmul_rn(x, 0x1p800);
     s = 0x1p-200;
   }
-  double r = __dsqrt_rn(__dsqrt_rn(x));
-  r = qrt_fix(x, r);
-  r = qrt_fix(x, r);
+  // sqrt(sqrt(x)) is within one ulp of x^(1/4): the inner rounding moves the
+  // root by at most 2^-54 relative (half an ulp at the top of a binade) and
+  // the outer rounding by half an ulp.  One correction therefore reaches the
+  // correctly rounded value.
+  const double r = qrt_fix(x, __dsqrt_rn(__dsqrt_rn(x)));
   return __dmul_rn(r, s);
 }
 

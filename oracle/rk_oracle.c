@@ -105,7 +105,7 @@ void oracle_rhs(int32_t rhs, int32_t dim, double t, const double* y,
 /* ------------------------------------------------------------------------ */
 /* x^(1/4) as a fixed sequence of IEEE-754 operations (sqrt, mul, sub, fma),
  * so that the CPU and the GPU produce the same bits.  It starts from
- * sqrt(sqrt(x)) (within 2 ulp) and applies two ulp-step corrections decided
+ * sqrt(sqrt(x)) (within one ulp) and applies one ulp-step correction decided
  * by the residual x - r^4, which is evaluated in double-double.  The result
  * is the correctly rounded fourth root except in cases where the root lies
  * within ~2^-50 ulp of a rounding midpoint. */
@@ -135,9 +135,8 @@ double oracle_qrt(double x) {
   double s = 1.0;
   if (x > 0x1p400) { x = x * 0x1p-800; s = 0x1p200; }
   else if (x < 0x1p-400) { x = x * 0x1p800; s = 0x1p-200; }
-  double r = sqrt(sqrt(x));
-  r = qrt_fix(x, r);
-  r = qrt_fix(x, r);
+  /* sqrt(sqrt(x)) is within one ulp of x^(1/4), so one correction suffices. */
+  const double r = qrt_fix(x, sqrt(sqrt(x)));
   return r * s;
 }
 
