@@ -114,6 +114,8 @@ SIGNATURES = {
     "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                               ctypes.POINTER(RkResult), ctypes.POINTER(Adjoint)]),
     "bacon_ctx_last_reverse_ms": (ctypes.c_int, [_VP, DP]),
+    "bacon_rk_solve_noalloc": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                              ctypes.POINTER(RkResult), _VP]),
     "bacon_builder_new": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),
     "bacon_builder_new_dyn": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),
     "bacon_builder_free": (None, [_VP]),

@@ -214,6 +214,33 @@ int bacon_rk_solve_adjoint(bacon_ctx* ctx, const bacon_problem* problem,
 /* Device time in milliseconds of the last adjoint's reverse kernel. */
 int bacon_ctx_last_reverse_ms(const bacon_ctx* ctx, double* ms);
 
+/* ---- allocation-free solve ------------------------------------------------ */
+/* No counterpart in the reference.  The batched solve of bacon_rk_solve for
+ * callers that cannot allocate device memory: a library inside an application
+ * whose memory pool has reserved the GPU's memory, a hot loop where an
+ * allocation's latency or failure is not acceptable, or plugin code that holds
+ * only a stream and device pointers.  It needs no bacon_ctx and calls no
+ * cudaMalloc, cudaFree or other allocating routine: its scratch (work
+ * counter, lowest-failing-index slot, longest-first order) is one fixed device
+ * array of about 4 MiB inside the library, which every GPU that loads the
+ * library holds until the process exits.
+ *   - options->memory must be BACON_MEM_DEVICE (every array on the device);
+ *     use_graph is ignored.
+ *   - At most 1,048,576 systems: a larger n returns BACON_CAPACITY_EXCEEDED
+ *     before any GPU work.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the one array, which keeps the last call's contents;
+ *     each call resets what must start at zero.  Calls whose GPU work overlaps
+ *     (other host threads or streams) race on it: serialize them.
+ *   - `stream` is a cudaStream_t (NULL: the legacy default stream).  The call
+ *     returns once the solve has finished; outputs as for bacon_rk_solve.
+ *   - Failures are reported through the return code only; bacon_last_error()
+ *     is not updated, because composing a message would allocate. */
+int bacon_rk_solve_noalloc(const bacon_problem* problem, const bacon_rk_options* options,
+                           bacon_rk_result* result, void* stream);
+
 /* Validate a problem the way the reference builder does (rk.rs:168-256):
  * tolerance, dt bounds, start/end order, missing parameters.  No GPU work. */
 int bacon_rk_validate(const bacon_problem* problem);
