@@ -86,6 +86,18 @@ class RkResult(ctypes.Structure):
     ]
 
 
+class BdfOptions(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("memory", ctypes.c_int32),
+        ("max_iter", ctypes.c_int32),
+        ("max_steps", ctypes.c_int64),
+        ("block", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+    ]
+
+
 class Adjoint(ctypes.Structure):
     _fields_ = [
         ("target", ctypes.c_void_p),
@@ -111,6 +123,10 @@ SIGNATURES = {
     "bacon_rk_solve_plain": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                             ctypes.POINTER(RkResult)]),
     "bacon_rk_validate": (ctypes.c_int, [ctypes.POINTER(Problem)]),
+    "bacon_bdf_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(BdfOptions),
+                                       ctypes.POINTER(RkResult)]),
+    "bacon_rk_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                         ctypes.POINTER(RkResult), I32P, I32P]),
     "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                               ctypes.POINTER(RkResult), ctypes.POINTER(Adjoint)]),
     "bacon_ctx_last_reverse_ms": (ctypes.c_int, [_VP, DP]),

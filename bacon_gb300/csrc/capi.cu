@@ -3,6 +3,7 @@
 // cache).  See include/bacon_gb300.h for the reference interfaces replaced.
 #include "bacon_gb300.h"
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -11,6 +12,11 @@
 #include <unordered_map>
 #include <vector>
 
+#include "bdf.h"
+#include "linear.cuh"
+#include "linear.h"
+#include "linear_tc.cuh"
+#include "bdf_kernel.cuh"
 #include "order.h"
 #include "plain.h"
 #include "registry.h"
@@ -118,7 +124,10 @@ struct bacon_ctx {
   cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the last adjoint reverse kernel
   bool rev_valid = false;
   std::vector<bacon::AdjEntry> adjoint_kernels;
+  std::vector<bacon::BdfEntry> bdf_kernels;
   DevBuf adj_dt, adj_ck, adj_tgt, adj_loss, adj_gy, adj_gp;
+  DevBuf lin_A, lin_y, lin_K, lin_t, lin_dt, lin_end, lin_att;
+  DevBuf tc_sa, tc_ea, tc_sy, tc_ey;
 };
 
 extern "C" {
@@ -163,7 +172,8 @@ int bacon_ctx_destroy(bacon_ctx* c) {
                     &c->out_acc, &c->out_rej, &c->out_st, &c->out_tt, &c->out_ty, &c->pl_y, &c->pl_K,
                     &c->pl_t, &c->pl_dt, &c->pl_end, &c->pl_att, &c->pl_acc, &c->pl_rej, &c->pl_st,
                     &c->ord, &c->ord_scratch, &c->adj_dt, &c->adj_ck, &c->adj_tgt, &c->adj_loss,
-                    &c->adj_gy, &c->adj_gp})
+                    &c->adj_gy, &c->adj_gp, &c->lin_A, &c->lin_y, &c->lin_K, &c->lin_t, &c->lin_dt,
+                    &c->lin_end, &c->lin_att, &c->tc_sa, &c->tc_ea, &c->tc_sy, &c->tc_ey})
     b->release();
   if (c->ev2) cudaEventDestroy(c->ev2);
   if (c->ev3) cudaEventDestroy(c->ev3);
@@ -234,6 +244,28 @@ int bacon_measure_fp64_peak(bacon_ctx* c, double* gflops) {
 }  // extern "C"
 
 namespace {
+
+// Occupancy model for the persistent kernels: the FP64 pipe is saturated by
+// two 128-thread CTAs per SM, while every extra resident thread lengthens the
+// tail in which lanes run out of systems.  Aim for >= 16 systems per thread
+// and at least 256 threads per SM.
+int model_blocks_per_sm(int64_t n, int num_sms, int block, int max_bps) {
+  const int64_t threads_for_tail = n / 16;
+  int64_t bps = threads_for_tail / (static_cast<int64_t>(num_sms) * block);
+  const int64_t floor_bps = (256 + block - 1) / block;
+  if (bps < floor_bps) bps = floor_bps;
+  if (bps > 4) bps = 4;
+  if (bps > max_bps) bps = max_bps;
+  return static_cast<int>(bps < 1 ? 1 : bps);
+}
+
+// Autotune cache key: the kernel and the batch size rounded to a power of two.
+uint64_t tune_key(const bacon::RkKey& k, int64_t n) {
+  int lg = 0;
+  while ((int64_t{1} << lg) < n && lg < 62) ++lg;
+  uint64_t h = fnv1a(&k, sizeof(k));
+  return fnv1a(&lg, sizeof(lg), h);
+}
 
 // Effective dt bounds after the builder's cross-clamping with minimum set
 // before maximum (with_minimum_dt then with_maximum_dt, rk.rs:179-210).
@@ -360,8 +392,169 @@ int batch_return_code(bacon_ctx* c, const bacon_rk_result* r, bool host, const R
 
 }  // namespace
 
+namespace {
+
+// Lock-step batched RKF45 for y' = A y with a shared A (linear.cuh): one
+// round = one attempt for every running system = S stage GEMMs + one
+// control kernel; the host relaunches the round until no system runs.
+int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt, bacon_rk_result* r) {
+  if (!p->shared) return fail(BACON_MISSING_PARAMETERS, "BACON_RHS_LINEAR needs the shared matrix");
+  if (r->traj_t) return fail(BACON_UNSUPPORTED, "the linear engine records no trajectory");
+  const bool tc = opt->precision == BACON_TC_SPLIT;
+  bacon::LinKernels k;
+  bacon::LinTcKernels tk;
+  if (!bacon::lin_kernels(opt->method, opt->layout, tc ? 0 : opt->precision, p->dim, k) ||
+      (tc && !bacon::lin_tc_kernels(opt->method, opt->layout, p->dim, tk)))
+    return fail(BACON_UNSUPPORTED, "linear engine: dim 64/128/256 (128/256 on tensor cores); layouts "
+                                   "as_written / fehlberg; precision FP64_EXACT, FP64_FMA or TC_SPLIT");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  int rc;
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  const size_t n = static_cast<size_t>(p->n), D = static_cast<size_t>(p->dim);
+  const double* A = p->shared;
+  if (host) {
+    BACON_CUDA(c->lin_A.ensure(D * D * sizeof(double)));
+    BACON_CUDA(cudaMemcpyAsync(c->lin_A.p, p->shared, D * D * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    A = c->lin_A.as<double>();
+    if ((rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+  }
+  BACON_CUDA(c->lin_y.ensure(n * D * sizeof(double)));
+  BACON_CUDA(c->lin_K.ensure(static_cast<size_t>(k.stages) * n * D * sizeof(double)));
+  BACON_CUDA(c->lin_t.ensure(n * sizeof(double)));
+  BACON_CUDA(c->lin_dt.ensure(n * sizeof(double)));
+  BACON_CUDA(c->lin_end.ensure(n * sizeof(double)));
+  BACON_CUDA(c->lin_att.ensure(n * sizeof(int64_t)));
+  double dt_min = p->dt_min;
+  clamp_dt(dt_min, p->dt_max);
+  bacon::LinArgs st{};
+  st.n = p->n;
+  st.A = A;
+  st.y = c->lin_y.as<double>();
+  st.K = c->lin_K.as<double>();
+  st.t = c->lin_t.as<double>();
+  st.dt = c->lin_dt.as<double>();
+  st.end = c->lin_end.as<double>();
+  st.attempts = c->lin_att.as<int64_t>();
+  st.accepted = o.acc;
+  st.rejected = o.rej;
+  st.status = o.st;
+  st.live = reinterpret_cast<unsigned int*>(c->d_ctl + 2);
+  st.tol = p->tol;
+  st.dt_min = dt_min;
+  st.dt_max = p->dt_max;
+  st.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  bacon::LinInitArgs ia{};
+  ia.st = st;
+  ia.dim = p->dim;
+  ia.stages = k.stages;
+  ia.y0 = o.y0;
+  ia.t0 = o.t0;
+  ia.t_end = o.t_end;
+  ia.t0_s = p->t0_scalar;
+  ia.t_end_s = p->t_end_scalar;
+  ia.dt0 = (p->dt_max + dt_min) * 0.5;
+  void* iargs[] = {&ia};
+  const unsigned ig = static_cast<unsigned>((n * D + 255) / 256);
+  BACON_CUDA(cudaLaunchKernel(k.init, dim3(ig), dim3(256), iargs, 0, c->stream));
+  unsigned int* h_live = reinterpret_cast<unsigned int*>(c->h_ctl + 2);
+  int first = 1;
+  void* cargs[] = {&st, &first};
+  void* sargs[] = {&st};
+  const unsigned cg = static_cast<unsigned>((n * 32 + 255) / 256);
+  const dim3 sg(static_cast<unsigned>((n + 63) / 64), static_cast<unsigned>(D / 64));
+  BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
+  BACON_CUDA(cudaLaunchKernel(k.control, dim3(cg), dim3(256), cargs, 0, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  c->launches += 2;
+  first = 0;
+  bacon::TcArgs ta{};
+  unsigned int* d_err = reinterpret_cast<unsigned int*>(c->d_ctl + 3);
+  if (tc) {
+    BACON_CUDA(c->tc_sa.ensure(static_cast<size_t>(tk.slices) * D * D * sizeof(__nv_bfloat16)));
+    BACON_CUDA(c->tc_ea.ensure(D * sizeof(int32_t)));
+    BACON_CUDA(c->tc_sy.ensure(static_cast<size_t>(tk.slices) * n * D * sizeof(__nv_bfloat16)));
+    BACON_CUDA(c->tc_ey.ensure(n * sizeof(int32_t)));
+    BACON_CUDA(cudaFuncSetAttribute(tk.gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, tk.smem_bytes));
+    ta.st = st;
+    ta.sa = c->tc_sa.as<__nv_bfloat16>();
+    ta.ea = c->tc_ea.as<int32_t>();
+    ta.sy = c->tc_sy.as<__nv_bfloat16>();
+    ta.ey = c->tc_ey.as<int32_t>();
+    ta.error_flag = d_err;
+    BACON_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned int), c->stream));
+    const double* Ap = A;
+    __nv_bfloat16* sa = c->tc_sa.as<__nv_bfloat16>();
+    int32_t* ea = c->tc_ea.as<int32_t>();
+    void* aargs[] = {&Ap, &sa, &ea};
+    BACON_CUDA(cudaLaunchKernel(tk.slice_a, dim3(static_cast<unsigned>((D * 32 + 255) / 256)), dim3(256), aargs, 0,
+                                c->stream));
+    c->launches += 1;
+  }
+  __nv_bfloat16* sy = c->tc_sy.as<__nv_bfloat16>();
+  int32_t* ey = c->tc_ey.as<int32_t>();
+  const dim3 tg(static_cast<unsigned>((n + bacon::kTcN - 1) / bacon::kTcN), static_cast<unsigned>(D / bacon::kTcM));
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  while (*h_live > 0) {
+    for (int s = 0; s < k.stages; ++s) {
+      if (tc) {
+        ta.stage = s;
+        void* slargs[] = {&ta, &sy, &ey};
+        BACON_CUDA(cudaLaunchKernel(tk.slice[s], dim3(cg), dim3(256), slargs, 0, c->stream));
+        void* gargs[] = {&ta};
+        BACON_CUDA(cudaLaunchKernel(tk.gemm, tg, dim3(256), gargs, static_cast<size_t>(tk.smem_bytes), c->stream));
+        c->launches += 1;
+      } else {
+        BACON_CUDA(cudaLaunchKernel(k.stage[s], sg, dim3(256), sargs, 0, c->stream));
+      }
+    }
+    BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
+    BACON_CUDA(cudaLaunchKernel(k.control, dim3(cg), dim3(256), cargs, 0, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaStreamSynchronize(c->stream));
+    c->launches += k.stages + 1;
+  }
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  c->ev_valid = true;
+  int dim = p->dim;
+  double* yo = o.y_out;
+  void* oargs[] = {&st, &dim, &yo};
+  BACON_CUDA(cudaLaunchKernel(k.output, dim3(ig), dim3(256), oargs, 0, c->stream));
+  BACON_CUDA(cudaMemcpyAsync(o.t_out, st.t, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  c->launches += 1;
+  if (host && (rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  if (tc) {
+    unsigned int herr = 0;
+    BACON_CUDA(cudaMemcpy(&herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost));
+    if (herr) return fail(BACON_CUDA_ERROR, "tensor-core stage: a bounded mbarrier wait gave up");
+  }
+  std::vector<int32_t> hs;
+  const int32_t* sp = r->status;
+  if (!host) {
+    hs.resize(n);
+    BACON_CUDA(cudaMemcpy(hs.data(), o.st, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    sp = hs.data();
+  }
+  for (size_t i = 0; i < n; ++i)
+    if (sp[i] != 0) return fail(sp[i], "system " + std::to_string(i) + " ended with status " + std::to_string(sp[i]));
+  return BACON_OK;
+}
+
+}  // namespace
+
 extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                               bacon_rk_result* r) {
+  if (c && opt && p && p->rhs == BACON_RHS_LINEAR) {
+    int rc0 = bacon_rk_validate(p);
+    if (rc0 != BACON_OK) return rc0;
+    if ((rc0 = check_result_ptrs(p, r)) != BACON_OK) return rc0;
+    return linear_solve(c, p, opt, r);
+  }
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   int rc = bacon_rk_validate(p);
   if (rc != BACON_OK) return rc;
@@ -422,12 +615,24 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
     a.order = oa.order;
   }
 
-  int block = opt->block > 0 ? opt->block : 128;
+  // Launch shape: explicit options, else the autotuned shape for this kernel
+  // and batch size (bacon_rk_autotune), else the occupancy model.
+  int block = opt->block > 0 ? opt->block : 0;
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 0;
+  const uint64_t tkey = tune_key(key, p->n);
+  if (block == 0 && bps == 0) {
+    auto it = c->tuned.find(tkey);
+    if (it != c->tuned.end()) {
+      block = it->second.first;
+      bps = it->second.second;
+    }
+  }
+  if (block == 0) block = 128;
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
   if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
-  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
+  if (bps == 0) bps = model_blocks_per_sm(p->n, c->num_sms, block, max_bps);
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(c->num_sms) * bps;
   const long long need = (p->n + block - 1) / block;
@@ -589,6 +794,112 @@ extern "C" int bacon_rk_solve_plain(bacon_ctx* c, const bacon_problem* p, const 
   }
   for (size_t i = 0; i < n; ++i)
     if (sp[i] != 0) return fail(sp[i], "system " + std::to_string(i) + " ended with status " + std::to_string(sp[i]));
+  return BACON_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched BDF (one system per thread, dim <= 8).
+extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon_bdf_options* opt,
+                               bacon_rk_result* r) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (opt->method != BACON_BDF6 && opt->method != BACON_BDF2) return fail(BACON_INVALID_ARGUMENT, "unknown method");
+  if (opt->mode != BACON_BDF_AS_COMPILED && opt->mode != BACON_BDF_CORRECTED)
+    return fail(BACON_INVALID_ARGUMENT, "unknown mode");
+  if (c->bdf_kernels.empty()) c->bdf_kernels = bacon::all_bdf_kernels();
+  const int want_method = (opt->mode == BACON_BDF_CORRECTED) ? 0 : opt->method;
+  const void* fn = nullptr;
+  for (const auto& e : c->bdf_kernels)
+    if (e.mode == opt->mode && e.method == want_method && e.rhs == p->rhs && e.dim == p->dim) fn = e.fn;
+  if (!fn) return fail(BACON_UNSUPPORTED, "no BDF kernel for this (mode, method, rhs, dim)");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  bacon::BdfArgs a{};
+  a.n = p->n;
+  a.y0 = o.y0;
+  a.params = o.params;
+  a.t0 = o.t0;
+  a.t_end = o.t_end;
+  a.t0_s = p->t0_scalar;
+  a.t_end_s = p->t_end_scalar;
+  a.tol = p->tol;
+  a.dt_min = p->dt_min;
+  a.dt_max = p->dt_max;
+  a.max_steps = opt->max_steps > 0 ? opt->max_steps : 10000000;
+  a.max_iter = opt->max_iter > 0 ? opt->max_iter : (opt->mode == BACON_BDF_CORRECTED ? 8 : 1000);
+  a.qmax = (opt->method == BACON_BDF6) ? 6 : 2;
+  a.y_out = o.y_out;
+  a.t_out = o.t_out;
+  a.accepted = o.acc;
+  a.rejected = o.rej;
+  a.status = o.st;
+  a.traj_t = o.traj_t;
+  a.traj_y = o.traj_y;
+  a.traj_cap = o.traj_t ? r->traj_cap : 0;
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+  int dyn = p->dyn_dim ? 1 : 0;
+  const int block = opt->block > 0 ? opt->block : 128;
+  if (block % 32 != 0 || block > 128) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 128");
+  int max_bps = 0;
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
+  if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : model_blocks_per_sm(p->n, c->num_sms, block, max_bps);
+  if (bps > max_bps) bps = max_bps;
+  long long grid = static_cast<long long>(c->num_sms) * bps;
+  const long long need = (p->n + block - 1) / block;
+  if (grid > need) grid = need;
+  if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+  void* args[] = {&a, &dyn};
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, 0, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  if (host && (rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+  c->launches += 1;
+  c->ev_valid = true;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  return batch_return_code(c, r, host, o);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: times the persistent kernel on the caller's own batch for a set
+// of launch shapes and caches the fastest for this kernel and batch size.
+extern "C" int bacon_rk_autotune(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                 bacon_rk_result* r, int32_t* best_block, int32_t* best_blocks_per_sm) {
+  if (!c || !opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  static const int kShapes[][2] = {{64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}};
+  bacon_rk_options o = *opt;
+  o.use_graph = 0;
+  double best_ms = 1e300;
+  int bb = 0, bs = 0;
+  for (const auto& sh : kShapes) {
+    o.block = sh[0];
+    o.blocks_per_sm = sh[1];
+    const int rc = bacon_rk_solve(c, p, &o, r);
+    if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+    double ms = 0.0;
+    if (bacon_ctx_last_kernel_ms(c, &ms) != BACON_OK) return BACON_CUDA_ERROR;
+    if (ms < best_ms) {
+      best_ms = ms;
+      bb = sh[0];
+      bs = sh[1];
+    }
+  }
+  const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
+  const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
+  c->tuned[tune_key(key, p->n)] = {bb, bs};
+  if (best_block) *best_block = bb;
+  if (best_blocks_per_sm) *best_blocks_per_sm = bs;
   return BACON_OK;
 }
 

@@ -1,0 +1,238 @@
+// Batched RKF45 for linear systems y' = A y with one shared dense A.
+//
+// All systems advance in lock-step rounds; a round is one attempt
+// (src/ivp/rk.rs:361-423) for every system still running.  The right-hand
+// side of a stage, K_i = dt * A * Y_i with Y_i = y + sum_j M(i,j) K_j, is a
+// GEMM over the batch: A (D x D) times the D x n matrix of stage inputs.
+// Each system keeps its own t, dt, accept/reject state and status.
+//
+// Layout in HBM: every per-system vector is contiguous, [n][D] (the GEMM's B
+// operand is then K-major), stage values K are [S][n][D], A is row-major.
+#pragma once
+
+#include <cstdint>
+
+#include "device_math.cuh"
+#include "rk_kernel.cuh"
+#include "tableau.cuh"
+
+namespace bacon {
+
+constexpr int32_t kLinRunning = -1;
+
+struct LinArgs {
+  int64_t n;
+  const double* A;     // [D][D] row-major
+  double* y;           // [n][D]  last yielded state
+  double* K;           // [S][n][D]
+  double* t;           // [n]
+  double* dt;          // [n]  dt of the attempt in flight (end-clamped)
+  double* end;         // [n]
+  int64_t* attempts;   // [n]
+  int32_t* accepted;   // [n]
+  int32_t* rejected;   // [n]
+  int32_t* status;     // [n]  kLinRunning while integrating
+  unsigned int* live;  // systems running after the control kernel
+  double tol, dt_min, dt_max;
+  int64_t max_attempts;
+};
+
+// ---------------------------------------------------------------------------
+// Stage kernel (FP64 SIMT GEMM): K_i[s][r] = dt_s * sum_k A[r][k] * Y_i[s][k].
+// 64 x 64 output tile (rows x systems), 256 threads with 4 x 4 outputs each;
+// the B tile is formed from y and the earlier stage values while it is
+// loaded.  Sums run over k in increasing order, so with ExactOps each output
+// equals the CPU oracle's matvec acc = acc + A[r][k] * y[k] bit for bit.
+template <class Ops, class Tab, int D, int STAGE>
+__global__ void __launch_bounds__(256) lin_stage_kernel(const LinArgs a) {
+  constexpr int TM = 64, TN = 64, TK = 16;
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN + 1];
+  const int r0 = blockIdx.y * TM;
+  const int64_t s0 = static_cast<int64_t>(blockIdx.x) * TN;
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int64_t n = a.n;
+
+  // Skip tiles whose systems have all finished.
+  __shared__ int any_running;
+  if (tid == 0) any_running = 0;
+  __syncthreads();
+  if (tid < TN && s0 + tid < n && a.status[s0 + tid] == kLinRunning) any_running = 1;
+  __syncthreads();
+  if (!any_running) return;
+
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  for (int k0 = 0; k0 < D; k0 += TK) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = tid + e * 256;  // 0..1023
+      const int rr = idx / TK, kk = idx % TK;
+      As[kk][rr] = a.A[static_cast<int64_t>(r0 + rr) * D + k0 + kk];
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = tid + e * 256;
+      const int ss = idx / TK, kk = idx % TK;
+      const int64_t sys = s0 + ss;
+      double v = 0.0;
+      if (sys < n) {
+        const int64_t off = sys * D + k0 + kk;
+        v = a.y[off];
+        static_for<0, Tab::S>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          constexpr double m = Tab::M(STAGE, j);
+          if constexpr (m != 0.0) v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], m);
+        });
+      }
+      Bs[kk][ss] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = Ops::axpy(acc[i][j], av[i], bv[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int64_t sys = s0 + tx * 4 + j;
+    if (sys >= n || a.status[sys] != kLinRunning) continue;
+    const double dts = a.dt[sys];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      a.K[(static_cast<int64_t>(STAGE) * n + sys) * D + r0 + ty * 4 + i] = Ops::mul(acc[i][j], dts);
+  }
+}
+
+// nalgebra norm of a dim >= 5 vector held by one warp: eight accumulators
+// over strides of 8 (blas.rs dotx), combined in its order.  Lanes 0..7 own
+// the accumulators; the result is valid in every lane.
+template <int D>
+__device__ __forceinline__ double warp_nalgebra_norm(const double* v, unsigned lane) {
+  static_assert(D >= 8 && D % 8 == 0, "dimension must be a multiple of 8");
+  double accl = 0.0;
+  if (lane < 8)
+    for (int i = 0; i < D; i += 8) accl = __dadd_rn(accl, __dmul_rn(v[i + lane], v[i + lane]));
+  double acc[8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l) acc[l] = __shfl_sync(0xffffffffu, accl, l);
+  double res = 0.0;
+  res = __dadd_rn(res, __dadd_rn(acc[0], acc[4]));
+  res = __dadd_rn(res, __dadd_rn(acc[1], acc[5]));
+  res = __dadd_rn(res, __dadd_rn(acc[2], acc[6]));
+  res = __dadd_rn(res, __dadd_rn(acc[3], acc[7]));
+  return __dsqrt_rn(__dadd_rn(0.0, res));
+}
+
+// Control kernel, one warp per system: finish the attempt in flight (error
+// estimate, accept, controller, dt_min check: rk.rs:386-416), then open the
+// next one (Done / attempt cap, end clamp: rk.rs:362-368).
+template <class Ops, class Tab, int D>
+__global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int first) {
+  constexpr int S = Tab::S;
+  constexpr int PER = D / 32;
+  const unsigned lane = threadIdx.x & 31u;
+  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  if (sys >= a.n) return;
+  if (a.status[sys] != kLinRunning) return;
+  const int64_t n = a.n;
+  double t = a.t[sys], dt = a.dt[sys];
+  const double end = a.end[sys];
+  int32_t st = kLinRunning;
+
+  if (!first) {
+    __shared__ double ev_s[8][D];
+    double* ev = ev_s[threadIdx.x / 32];
+    double yv[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int d = lane + 32 * q;
+      const int64_t off = sys * D + d;
+      double e = 0.0;
+      if constexpr (Tab::e(0) != 0.0) e = Ops::mul(a.K[off], Tab::e(0));
+      static_for<1, S>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        if constexpr (Tab::e(j) != 0.0) e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::e(j));
+      });
+      ev[d] = e;
+      yv[q] = a.y[off];
+    }
+    __syncwarp();
+    const double err = Ops::div(warp_nalgebra_norm<D>(ev, lane), dt);
+    const bool ok = err <= a.tol;
+    const double tn = ok ? Ops::add(t, dt) : t;
+    const double delta = qrt(Ops::div(a.tol, err));
+    double ndt;
+    if (delta <= 0.1) ndt = Ops::mul(dt, 0.1);
+    else if (delta >= 4.0) ndt = Ops::mul(dt, 4.0);
+    else ndt = Ops::mul(dt, delta);
+    if (ndt > a.dt_max) ndt = a.dt_max;
+    if (ndt < a.dt_min && tn < end) {
+      st = kStMinDt;
+    } else if (ok) {
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int d = lane + 32 * q;
+        const int64_t off = sys * D + d;
+        double v = yv[q];
+        static_for<0, S>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          if constexpr (Tab::b(j) != 0.0) v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::b(j));
+        });
+        a.y[off] = v;
+      }
+      t = tn;
+      if (lane == 0) a.accepted[sys] += 1;
+    } else {
+      if (lane == 0) a.rejected[sys] += 1;
+    }
+    dt = ndt;
+  }
+  if (st == kLinRunning) {
+    if (t >= end) {
+      st = (first && a.attempts[sys] == 0) ? kStTimeEndOob : kStOk;
+    } else if (a.attempts[sys] >= a.max_attempts) {
+      st = kStMaxAttempts;
+    } else {
+      if (Ops::add(t, dt) >= end) dt = Ops::sub(end, t);
+    }
+  }
+  if (lane == 0) {
+    a.t[sys] = t;
+    a.dt[sys] = dt;
+    if (st != kLinRunning) {
+      a.status[sys] = st;
+    } else {
+      a.attempts[sys] += 1;
+      atomicAdd(a.live, 1u);
+    }
+  }
+}
+
+}  // namespace bacon
+
+namespace bacon {
+struct LinInitArgs {
+  LinArgs st;
+  int dim;
+  int stages;
+  const double* y0;     // [D][n] SoA
+  const double* t0;
+  const double* t_end;
+  double t0_s, t_end_s, dt0;
+};
+}  // namespace bacon

@@ -1,0 +1,47 @@
+// Instantiations of the tensor-core (split-precision) stage GEMM of the
+// linear engine.
+#include <cuda_bf16.h>
+
+#include "linear.h"
+#include "linear_tc.cuh"
+
+namespace bacon {
+
+namespace {
+template <class Tab, int D>
+void fill_tc(LinTcKernels& k) {
+  k.slice_a = reinterpret_cast<const void*>(&lin_tc_slice_a_kernel<D>);
+  k.slice[0] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 0>);
+  k.slice[1] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 1>);
+  k.slice[2] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 2>);
+  k.slice[3] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 3>);
+  if constexpr (Tab::S > 4) {
+    k.slice[4] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 4>);
+    k.slice[5] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 5>);
+  }
+  k.gemm = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D>);
+  k.smem_bytes = kTcSlices * (kTcM * kTcKc * 2 + kTcN * kTcKc * 2);
+  k.slices = kTcSlices;
+}
+
+template <int D>
+bool pick(int method, int layout, LinTcKernels& k) {
+  if (method == 0) {
+    if (layout == 1) fill_tc<Tableau<Rkf45Literal, kAsWritten>, D>(k);
+    else if (layout == 2) fill_tc<Tableau<Rkf45Literal, kFehlberg>, D>(k);
+    else return false;
+  } else {
+    if (layout == 1 || layout == 2) fill_tc<Tableau<Bs23Literal, kAsWritten>, D>(k);
+    else return false;
+  }
+  return true;
+}
+}  // namespace
+
+bool lin_tc_kernels(int method, int layout, int dim, LinTcKernels& k) {
+  if (dim == 128) return pick<128>(method, layout, k);
+  if (dim == 256) return pick<256>(method, layout, k);
+  return false;
+}
+
+}  // namespace bacon

@@ -1,0 +1,313 @@
+// Tensor-core stage GEMM for the linear (shared-A) engine: split-precision
+// emulation of the FP64 product A * Y on tcgen05 (bf16 operands, FP32
+// accumulators in tensor memory).
+//
+// Splitting (the Ozaki scheme): every row of A and every system's stage
+// vector (a column of Y) is scaled by a power of two so that its largest
+// entry is below 1, then cut into NS slices of 6 bits each:
+//     x = 2^e * sum_s q_s 2^(-6(s+1)),  q_s integer, |q_s| <= 63.
+// Integers of at most 8 significant bits are exact in bf16, and a K = 256 dot
+// product of two slices is an integer below 256 * 63 * 63 < 2^20, so the
+// tensor cores compute every slice product exactly in FP32.  All pairs
+// (s, t) with s + t = d share the scale 2^(-6(d+2)); their sum stays below
+// 6 * 2^20 < 2^24 and is still exact, so one TMEM accumulator per diagonal d
+// (d = 0..NS-1) suffices.  The epilogue combines the NS diagonals in FP64,
+// applies 2^(e_row + e_sys) and the system's dt, and writes K_i.  Pairs with
+// s + t >= NS are dropped: the relative error of the product is ~2^(-6 NS).
+//
+// CTA tile: 128 rows of A x 64 systems, K = 256 in four chunks of 64 staged
+// in shared memory in the canonical no-swizzle K-major layout (8 x 16-byte
+// core matrices).  One thread issues the MMAs (M128 N64 K16), commits them to
+// an mbarrier, and every wait on it is bounded.
+#pragma once
+
+#include <cstdint>
+
+#include "linear.cuh"
+
+namespace bacon {
+
+constexpr int kTcSlices = 6;      // slices per operand (36 bits)
+constexpr int kTcBits = 6;        // bits per slice
+constexpr int kTcM = 128;         // rows per CTA
+constexpr int kTcN = 64;          // systems per CTA
+constexpr int kTcKc = 64;         // K per shared-memory chunk
+constexpr int kTcTmemCols = 512;  // kTcSlices accumulators x 64 columns, rounded to a power of two
+
+struct TcArgs {
+  LinArgs st;
+  const __nv_bfloat16* sa;  // [NS][D][D]   slices of A (row r, column k)
+  const int32_t* ea;        // [D]          row exponents of A
+  const __nv_bfloat16* sy;  // [NS][n][D]   slices of the stage inputs (system, component)
+  const int32_t* ey;        // [n]          system exponents
+  int stage;
+  unsigned int* error_flag; // set when a bounded wait gives up
+};
+
+// --- PTX wrappers -----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major: lbo = byte distance
+// between core matrices along K, sbo = along M/N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= static_cast<uint64_t>(1) << 46;  // descriptor version for tcgen05
+  return d;                             // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor for kind::f16: F32 accumulators, bf16 A and B, both
+// K-major, M = 128, N = 64.
+__host__ __device__ constexpr uint32_t tc_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(kTcN >> 3) << 17) |
+         (static_cast<uint32_t>(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase, unsigned int* error_flag) {
+  for (long long it = 0; it < (1ll << 26); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  atomicExch(error_flag, 1u);
+  return false;
+}
+
+// 16 consecutive 32-bit TMEM columns of this warp's 32 lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// --- the stage GEMM ------------------------------------------------------------
+// Shared memory: A slices for one chunk [NS][128 x 64] (16 KiB each), B slices
+// [NS][64 x 64] (8 KiB each): 144 KiB, plus the mbarrier and TMEM address.
+template <int D>
+__global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  constexpr int kABytes = kTcM * kTcKc * 2;  // 16384
+  constexpr int kBBytes = kTcN * kTcKc * 2;  // 8192
+  unsigned char* sA = tc_smem;
+  unsigned char* sB = tc_smem + kTcSlices * kABytes;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int any_running;
+
+  const int tid = threadIdx.x;
+  const int warp = tid / 32;
+  const int r0 = blockIdx.y * kTcM;
+  const int64_t s0 = static_cast<int64_t>(blockIdx.x) * kTcN;
+  const int64_t n = a.st.n;
+
+  if (tid == 0) any_running = 0;
+  __syncthreads();
+  if (tid < kTcN && s0 + tid < n && a.st.status[s0 + tid] == kLinRunning) any_running = 1;
+  __syncthreads();
+  if (!any_running) return;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_sh)),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+  const uint32_t mb = smem_addr(&mbar);
+  uint32_t phase = 0;
+  bool ok = true;
+
+  for (int kc = 0; kc < D; kc += kTcKc) {
+    // Stage the chunk: 16-byte vectors (8 bf16 along K) into core matrices.
+    for (int v = tid; v < kTcSlices * kTcM * (kTcKc / 8); v += 256) {
+      const int s = v / (kTcM * (kTcKc / 8));
+      const int rem = v % (kTcM * (kTcKc / 8));
+      const int m = rem / (kTcKc / 8), kg = rem % (kTcKc / 8);
+      const uint4 val = *reinterpret_cast<const uint4*>(
+          a.sa + (static_cast<int64_t>(s) * D + r0 + m) * D + kc + kg * 8);
+      *reinterpret_cast<uint4*>(sA + s * kABytes + (m / 8) * 1024 + kg * 128 + (m % 8) * 16) = val;
+    }
+    for (int v = tid; v < kTcSlices * kTcN * (kTcKc / 8); v += 256) {
+      const int s = v / (kTcN * (kTcKc / 8));
+      const int rem = v % (kTcN * (kTcKc / 8));
+      const int c = rem / (kTcKc / 8), kg = rem % (kTcKc / 8);
+      const int64_t sys = s0 + c;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (sys < n) val = *reinterpret_cast<const uint4*>(a.sy + (static_cast<int64_t>(s) * n + sys) * D + kc + kg * 8);
+      *reinterpret_cast<uint4*>(sB + s * kBBytes + (c / 8) * 1024 + kg * 128 + (c % 8) * 16) = val;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      constexpr uint32_t idesc = tc_idesc();
+#pragma unroll 1
+      for (int ks = 0; ks < kTcKc / 16; ++ks) {
+        for (int s = 0; s < kTcSlices; ++s) {
+          for (int t = 0; s + t < kTcSlices; ++t) {
+            const int d = s + t;
+            const uint64_t ad = umma_desc(smem_addr(sA + s * kABytes + ks * 256), 128, 1024);
+            const uint64_t bd = umma_desc(smem_addr(sB + t * kBBytes + ks * 256), 128, 1024);
+            // The first product into diagonal d is the pair (0, d) of the first
+            // K step: it overwrites the accumulator, every later one adds.
+            const uint32_t acc = (kc == 0 && ks == 0 && s == 0) ? 0u : 1u;
+            tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+          }
+        }
+      }
+      tc_commit(mb);
+    }
+    if (!mbar_wait_bounded(mb, phase, a.error_flag)) ok = false;
+    phase ^= 1u;
+    __syncthreads();
+    if (!ok) break;
+  }
+
+  // Epilogue: warps 0..3 own TMEM lanes (rows) 32w..32w+31, warps 4..7 the
+  // same rows for the second half of the 64 columns.
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int rw = warp % 4;
+    const int row = r0 + rw * 32 + (tid % 32);
+    const int cbase = (warp / 4) * 32;
+    const int erow = a.ea[row];
+    for (int cb = cbase; cb < cbase + 32; cb += 16) {
+      double accd[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) accd[j] = 0.0;
+      for (int d = kTcSlices - 1; d >= 0; --d) {
+        float v[16];
+        tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cb), v);
+        const double scale = ldexp(1.0, -kTcBits * (d + 2));
+#pragma unroll
+        for (int j = 0; j < 16; ++j) accd[j] = fma(static_cast<double>(v[j]), scale, accd[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int64_t sys = s0 + cb + j;
+        if (sys >= n || a.st.status[sys] != kLinRunning) continue;
+        const double f = ldexp(accd[j], erow + a.ey[sys]);
+        a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = f * a.st.dt[sys];
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+  }
+}
+
+// Slices of the stage inputs Y_i = y + sum_j M(i,j) K_j, one warp per system:
+// exponent e with max|Y| < 2^e, then q_s = trunc(Y * 2^(6(s+1) - e) - carried).
+template <class Tab, int D, int STAGE>
+__global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_bfloat16* sy, int32_t* ey) {
+  constexpr int PER = D / 32;
+  const unsigned lane = threadIdx.x & 31u;
+  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  const int64_t n = a.st.n;
+  if (sys >= n || a.st.status[sys] != kLinRunning) return;
+  double v[PER];
+  double mx = 0.0;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int64_t off = sys * D + lane + 32 * q;
+    double x = a.st.y[off];
+    static_for<0, Tab::S>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      constexpr double m = Tab::M(STAGE, j);
+      if constexpr (m != 0.0) x = fma(a.st.K[(static_cast<int64_t>(j) * n) * D + off], m, x);
+    });
+    v[q] = x;
+    mx = fmax(mx, fabs(x));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) {
+    frexp(mx, &e);  // mx < 2^e
+  }
+  if (lane == 0) ey[sys] = e;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    double r = ldexp(v[q], -e);  // |r| < 1
+#pragma unroll
+    for (int s = 0; s < kTcSlices; ++s) {
+      r = ldexp(r, kTcBits);
+      const double qs = trunc(r);
+      r -= qs;
+      sy[(static_cast<int64_t>(s) * n + sys) * D + lane + 32 * q] = __double2bfloat16(qs);
+    }
+  }
+}
+
+// Slices of A, one warp per row (computed once per solve).
+template <int D>
+__global__ void __launch_bounds__(256) lin_tc_slice_a_kernel(const double* A, __nv_bfloat16* sa, int32_t* ea) {
+  constexpr int PER = D / 32;
+  const unsigned lane = threadIdx.x & 31u;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if (row >= D) return;
+  double v[PER], mx = 0.0;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    v[q] = A[static_cast<int64_t>(row) * D + lane + 32 * q];
+    mx = fmax(mx, fabs(v[q]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);
+  if (lane == 0) ea[row] = e;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    double r = ldexp(v[q], -e);
+#pragma unroll
+    for (int s = 0; s < kTcSlices; ++s) {
+      r = ldexp(r, kTcBits);
+      const double qs = trunc(r);
+      r -= qs;
+      sa[(static_cast<int64_t>(s) * D + row) * D + lane + 32 * q] = __double2bfloat16(qs);
+    }
+  }
+}
+
+}  // namespace bacon

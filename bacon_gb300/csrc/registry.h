@@ -39,6 +39,7 @@ void register_rk45_exact_l1(std::vector<RkEntry>& v);
 void register_rk45_exact_l2(std::vector<RkEntry>& v);
 void register_rk45_fma(std::vector<RkEntry>& v);
 void register_rk23(std::vector<RkEntry>& v);
+void register_rk_ff(std::vector<RkEntry>& v);
 void register_adjoint_rk45(std::vector<AdjEntry>& v);
 void register_adjoint_rk23(std::vector<AdjEntry>& v);
 
@@ -49,6 +50,7 @@ inline std::vector<RkEntry> all_rk_kernels() {
   register_rk45_exact_l2(v);
   register_rk45_fma(v);
   register_rk23(v);
+  register_rk_ff(v);
   return v;
 }
 

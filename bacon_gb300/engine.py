@@ -17,7 +17,7 @@ from . import _capi
 
 RK45, RK23 = 0, 1
 AS_COMPILED, AS_WRITTEN, FEHLBERG = 0, 1, 2
-FP64_EXACT, FP64_FMA, FP32_COMP = 0, 1, 2
+FP64_EXACT, FP64_FMA, FP32_COMP, TC_SPLIT = 0, 1, 2, 3
 MEM_DEVICE, MEM_HOST = 0, 1
 
 
@@ -120,7 +120,7 @@ def _is_device(a) -> bool:
     return not isinstance(a, np.ndarray) and getattr(a, "is_cuda", False)
 
 
-def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False):
+def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False, shared=None):
     """Build a bacon_problem; t0 / t_end may be scalars or per-system arrays."""
     dim, n = int(y0.shape[0]), int(y0.shape[1])
     p = _capi.Problem()
@@ -141,7 +141,7 @@ def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False)
         p.t_end_scalar = float(t_end)
     else:
         p.t_end = _ptr(t_end)
-    p.shared = None
+    p.shared = _ptr(shared)
     p.tol, p.dt_min, p.dt_max = float(tol), float(dt_min), float(dt_max)
     return p
 
@@ -200,8 +200,9 @@ def make_result(out, traj_cap=0):
 def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
              precision=FP64_EXACT, max_attempts=0, traj_cap=0, ctx: Context | None = None,
              plain=False, block=0, blocks_per_sm=0, use_graph=True, dyn_dim=False, out=None,
-             raise_on_error=False, schedule=0) -> Solution:
-    """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors."""
+             raise_on_error=False, schedule=0, shared=None) -> Solution:
+    """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors.
+    ``shared``: the dim x dim matrix of BACON_RHS_LINEAR (row-major)."""
     ctx = ctx or default_context()
     device = _is_device(y0)
     if not device:
@@ -212,8 +213,10 @@ def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, la
             t0 = np.ascontiguousarray(t0, dtype=np.float64)
         if not np.isscalar(t_end):
             t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    if shared is not None and not device:
+        shared = np.ascontiguousarray(shared, dtype=np.float64)
     dim, n = int(y0.shape[0]), int(y0.shape[1])
-    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim)
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim, shared)
     opts = rk_options(method, layout, precision, MEM_DEVICE if device else MEM_HOST, max_attempts,
                       block, blocks_per_sm, use_graph, schedule)
     if out is None:
@@ -283,3 +286,57 @@ def rk_solve_adjoint(y0, params, t0, t_end, target, *, rhs, tol, dt_min, dt_max,
     fwd = Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code))
     return AdjointSolution(fwd, grads["loss"], grads["dl_dy0"], grads["dl_dp"] if n_params else None,
                            int(code))
+
+
+def rk_autotune(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
+                precision=FP64_EXACT, max_attempts=0, ctx: Context | None = None, out=None,
+                schedule=0) -> tuple[int, int]:
+    """Time the candidate launch shapes on this batch and cache the fastest in
+    the context (used by later solves of the same kernel and batch size).
+    Returns (threads per block, persistent CTAs per SM)."""
+    ctx = ctx or default_context()
+    device = _is_device(y0)
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs)
+    opts = rk_options(method, layout, precision, MEM_DEVICE if device else MEM_HOST, max_attempts,
+                      0, 0, False, schedule)
+    if out is None:
+        out = alloc_outputs(dim, n, device)
+    res = make_result(out)
+    bb, bs = ctypes.c_int32(), ctypes.c_int32()
+    check(_capi.load().bacon_rk_autotune(ctx.handle, ctypes.byref(prob), ctypes.byref(opts),
+                                         ctypes.byref(res), ctypes.byref(bb), ctypes.byref(bs)))
+    return bb.value, bs.value
+
+
+BDF6, BDF2 = 0, 1
+BDF_AS_COMPILED, BDF_CORRECTED = 0, 1
+
+
+def bdf_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=BDF6, mode=BDF_CORRECTED,
+              max_iter=0, max_steps=0, traj_cap=0, ctx: Context | None = None, block=0, blocks_per_sm=0,
+              dyn_dim=False, out=None, raise_on_error=False) -> Solution:
+    """Batched BDF6 / BDF2 solve (systems of dimension <= 8)."""
+    ctx = ctx or default_context()
+    device = _is_device(y0)
+    if not device:
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        if params is not None:
+            params = np.ascontiguousarray(params, dtype=np.float64)
+        if not np.isscalar(t0):
+            t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        if not np.isscalar(t_end):
+            t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim)
+    o = _capi.BdfOptions()
+    o.method, o.mode, o.memory = method, mode, MEM_DEVICE if device else MEM_HOST
+    o.max_iter, o.max_steps, o.block, o.blocks_per_sm = int(max_iter), int(max_steps), int(block), int(blocks_per_sm)
+    if out is None:
+        out = alloc_outputs(dim, n, device, traj_cap)
+    res = make_result(out, traj_cap)
+    code = _capi.load().bacon_bdf_solve(ctx.handle, ctypes.byref(prob), ctypes.byref(o), ctypes.byref(res))
+    if code in (14, 15, 16) or (raise_on_error and code != 0):
+        raise IVPError(code, _capi.last_error())
+    return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code),
+                    out.get("traj_t"), out.get("traj_y"))

@@ -29,7 +29,7 @@ from . import _capi
 from .engine import (AS_COMPILED, AS_WRITTEN, FEHLBERG, FP32_COMP, FP64_EXACT, FP64_FMA, RK23, RK45,
                      Context, IVPError, Solution, check, rk_solve)
 
-__all__ = ["Rhs", "RungeKutta45", "RungeKutta23", "IVPError", "IVPIterator", "AS_COMPILED",
+__all__ = ["Rhs", "RungeKutta45", "RungeKutta23", "BDF6", "BDF2", "IVPError", "IVPIterator", "AS_COMPILED",
            "AS_WRITTEN", "FEHLBERG", "FP64_EXACT", "FP64_FMA", "FP32_COMP"]
 
 
@@ -220,6 +220,55 @@ class _RkBuilder:
                 break
             cap = int(np.max(sol.accepted)) + 1
         return IVPIterator(sol, n, dim)
+
+
+class _BdfBuilder(_RkBuilder):
+    """BDF builder (src/ivp/bdf.rs:124-332): same trait methods as the
+    Runge-Kutta builders; ``solve`` runs the batched BDF kernels."""
+    KIND = 2
+    BDF_METHOD = 0
+
+    def solve(self, data=None, *, mode: int | None = None, max_iter: int = 0, max_steps: int = 0,
+              record_path: bool | None = None, path_capacity: int = 4096,
+              ctx: Context | None = None, **_ignored) -> IVPIterator:
+        """Run every system on the GPU.  ``mode``: BDF_CORRECTED (default) or
+        BDF_AS_COMPILED (the reference's 0.16.2 behaviour)."""
+        from .engine import BDF_CORRECTED, bdf_solve
+        mode = BDF_CORRECTED if mode is None else mode
+        prob = _capi.Problem()
+        check(self._lib.bacon_builder_problem(self._h, ctypes.byref(prob)))
+        n, dim = int(prob.n), int(prob.dim)
+        y0 = np.ctypeslib.as_array(ctypes.cast(prob.y0, _capi.DP), shape=(dim, n)).copy()
+        params = None
+        if prob.n_params:
+            params = np.ctypeslib.as_array(ctypes.cast(prob.params, _capi.DP), shape=(prob.n_params, n)).copy()
+        t_end = prob.t_end_scalar
+        if prob.t_end:
+            t_end = np.ctypeslib.as_array(ctypes.cast(prob.t_end, _capi.DP), shape=(n,)).copy()
+        if record_path is None:
+            record_path = n <= 64
+        cap = path_capacity if record_path else 0
+        while True:
+            sol = bdf_solve(y0, params, prob.t0_scalar, t_end, rhs=prob.rhs, tol=prob.tol,
+                            dt_min=prob.dt_min, dt_max=prob.dt_max, method=self.BDF_METHOD, mode=mode,
+                            max_iter=max_iter, max_steps=max_steps, traj_cap=cap, ctx=ctx,
+                            dyn_dim=bool(prob.dyn_dim))
+            if not cap or int(np.max(sol.accepted)) <= cap:
+                break
+            cap = int(np.max(sol.accepted)) + 1
+        return IVPIterator(sol, n, dim)
+
+
+class BDF6(_BdfBuilder):
+    """Sixth-order BDF (src/ivp/bdf.rs:641-706)."""
+    KIND = 2
+    BDF_METHOD = 0
+
+
+class BDF2(_BdfBuilder):
+    """Second-order BDF (src/ivp/bdf.rs:708-762)."""
+    KIND = 3
+    BDF_METHOD = 1
 
 
 class RungeKutta45(_RkBuilder):

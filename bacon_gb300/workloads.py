@@ -92,3 +92,39 @@ def robertson(n: int = 1 << 16, seed: int = 5) -> Batch:
     y0[0] = 1.0
     return Batch("robertson", RHS_ROBERTSON, y0, np.stack([k1, k2, k3]), np.zeros(n),
                  np.full(n, 1e4), 1e-6, 1e-10, 1e3, seed)
+
+
+def spring_chains(n: int = 1 << 15, masses: int = 4, seed: int = 6) -> Batch:
+    """Damped spring-mass chains with `masses` unit masses (dim 2*masses):
+    stiffness k_i = 10^U[0, 6] (ratio up to 1e6), damping c = 2 sqrt(max k)
+    on every mass (critical for the stiffest spring, so the stiff modes are
+    real and decaying), x0 ~ U[-1, 1], v0 = 0, t in [0, 10], tol 1e-6.
+    Damping, end time and dt bounds (1e-12 .. 1) are not given by the
+    workload description and are chosen here."""
+    rng = np.random.default_rng(seed)
+    k = 10.0 ** rng.uniform(0.0, 6.0, (masses, n))
+    c = 2.0 * np.sqrt(k.max(axis=0))
+    y0 = np.zeros((2 * masses, n))
+    y0[:masses] = rng.uniform(-1.0, 1.0, (masses, n))
+    return Batch(f"spring_chain_{masses}", RHS_CHAIN, y0, np.concatenate([k, c[None, :]]), np.zeros(n),
+                 np.full(n, 10.0), 1e-6, 1e-12, 1.0, seed)
+
+
+def linear_shared(n: int = 1 << 16, dim: int = 256, seed: int = 4) -> Batch:
+    """y' = A y with one shared A = Q diag(-lambda) Q^T (Q orthogonal from the
+    QR factorisation of a Gaussian matrix, lambda log-uniform in [1e-2, 1e1]),
+    y0 ~ N(0, I), t in [0, 5], tol 1e-8.  dt bounds chosen: 1e-10 .. 0.1.
+    The exact solution is Q diag(exp(-lambda t)) Q^T y0 (extra["exact"])."""
+    rng = np.random.default_rng(seed)
+    q, r = np.linalg.qr(rng.normal(size=(dim, dim)))
+    q = q * np.sign(np.diag(r))
+    lam = 10.0 ** rng.uniform(-2.0, 1.0, dim)
+    A = (q * -lam) @ q.T
+    y0 = rng.normal(size=(dim, n))
+
+    def exact(t: float, cols=slice(None)):
+        return q @ (np.exp(-lam * t)[:, None] * (q.T @ y0[:, cols]))
+
+    return Batch("linear_shared", RHS_LINEAR, y0, np.zeros((0, n)), np.zeros(n), np.full(n, 5.0),
+                 1e-8, 1e-10, 0.1, seed, {"A": np.ascontiguousarray(A), "Q": q, "lambda": lam,
+                                          "exact": exact})

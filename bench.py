@@ -281,6 +281,70 @@ def main():
             "what": "one launch per attempt, state in HBM, dense tableau, host loop until done"}
         extras["speedup_vs_plain"] = value / world / (b.n / plain_s)
 
+        # FP32-stage mode (float-float stages, FP64 control), same workload.
+        cout = E.alloc_outputs(3, b.n, device=True)
+        solve(E.FP32_COMP, cout)
+        comp_ms = []
+        for _ in range(2):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            solve(E.FP32_COMP, cout)
+            comp_ms.append(ctx.last_kernel_ms())
+        comp_value = b.n / (min(comp_ms) * 1e-3)
+        extras["fp32_comp_mode"] = {"value": comp_value, "unit": UNIT,
+                                    "speedup_vs_fp64_exact": comp_value / (value / world),
+                                    "speedup_vs_plain": comp_value / (b.n / plain_s),
+                                    "what": "float-float stages on the FP32 pipe, FP64 accept test and dt"}
+
+        # Final-state error against FP64 DOP853 at rtol 1e-12 (sample: T <= 5).
+        from bacon_gb300 import accuracy as A
+        short = np.flatnonzero(b.t_end <= 5.0)[:32]
+        sb = b.subset(short)
+        ref = A.reference_final_states(sb)
+        extras["final_state_error_vs_rtol1e-12"] = {
+            "fp64_exact": A.final_state_error(out["y"].cpu().numpy()[:, short], ref),
+            "fp32_comp": A.final_state_error(cout["y"].cpu().numpy()[:, short], ref),
+            "sample": f"{short.size} Lorenz systems with T <= 5 (chaotic: error grows with T)"}
+
+        # Discrete adjoint (batched solve_ivp_adjoint) on the Lotka-Volterra workload.
+        from bacon_gb300 import workloads as W
+        lv = W.lotka_volterra()
+        ly0, lprm, ltg = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+                          for x in (lv.y0, lv.params, lv.extra["target"]))
+        lout = E.alloc_outputs(2, lv.n, device=True)
+        kw = dict(rhs=lv.rhs, tol=lv.tol, dt_min=lv.dt_min, dt_max=lv.dt_max, ctx=ctx, out=lout)
+        E.rk_solve(ly0, lprm, 0.0, 15.0, layout=E.FEHLBERG, **kw)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        E.rk_solve(ly0, lprm, 0.0, 15.0, layout=E.FEHLBERG, **kw)
+        fwd_ms = ctx.last_kernel_ms()
+        adj = E.rk_solve_adjoint(ly0, lprm, 0.0, 15.0, ltg, layout=E.FEHLBERG, **kw)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        adj = E.rk_solve_adjoint(ly0, lprm, 0.0, 15.0, ltg, layout=E.FEHLBERG, **kw)
+        adj_wall = time.perf_counter() - s0
+        rec_ms, rev_ms = ctx.last_kernel_ms(), ctx.last_reverse_ms()
+        adj_ms = rec_ms + rev_ms
+        grad = torch.cat([adj.dl_dy0, adj.dl_dp]).cpu().numpy()
+        fd_rel = None
+        if rank == 0:
+            from oracle import oracle as O
+            cfg = O.rk_cfg(layout=O.FEHLBERG, tol=lv.tol, dt_min=lv.dt_min, dt_max=lv.dt_max)
+            worst = 0.0
+            for i in range(0, lv.n, lv.n // 16):
+                _, fy, fp = O.rk_frozen_fd_one(cfg, lv.rhs, lv.y0[:, i], lv.params[:, i], 0.0, 15.0,
+                                               lv.extra["target"][:, i], 1e-6)
+                g = grad[:, i]
+                worst = max(worst, float(np.abs(g - np.concatenate([fy, fp])).max() / np.abs(g).max()))
+            fd_rel = worst
+        extras["adjoint"] = {
+            "value": lv.n / (adj_ms * 1e-3), "unit": "grads/s", "workload": "Lotka-Volterra, 262144 systems, "
+            "t in [0,15], tol 1e-7, loss = sum ||y(T)-target||^2, checkpoint every 32 accepted steps",
+            "e2e_value": lv.n / adj_wall, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+            "record_forward_ms": rec_ms, "reverse_ms": rev_ms, "cost_vs_forward": adj_ms / fwd_ms,
+            "max_rel_diff_vs_frozen_central_fd_h1e-6": fd_rel, "fd_sample": 16}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",

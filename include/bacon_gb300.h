@@ -94,7 +94,11 @@ typedef enum {
 typedef enum {
   BACON_FP64_EXACT = 0,
   BACON_FP64_FMA = 1,
-  BACON_FP32_COMP = 2
+  BACON_FP32_COMP = 2,
+  /* BACON_RHS_LINEAR only: the stage GEMM on tcgen05 tensor cores, bf16
+   * integer slices of A and Y (6 x 6 bits, Ozaki splitting) with exact FP32
+   * accumulation, combined in FP64; relative error of A*Y ~ 2^-36. */
+  BACON_TC_SPLIT = 3
 } bacon_precision;
 
 typedef enum { BACON_MEM_DEVICE = 0, BACON_MEM_HOST = 1 } bacon_memory;
@@ -183,11 +187,51 @@ typedef struct {
 int bacon_rk_solve(bacon_ctx* ctx, const bacon_problem* problem,
                    const bacon_rk_options* options, bacon_rk_result* result);
 
+/* Autotuner: runs bacon_rk_solve on this batch with each candidate launch
+ * shape (threads per block x persistent CTAs per SM), times the integration
+ * kernel with CUDA events, and caches the fastest in the context for this
+ * kernel and batch size (rounded to a power of two).  Later solves that leave
+ * block and blocks_per_sm at 0 use it; without tuning an occupancy model
+ * applies.  The result arrays receive the last candidate's (identical)
+ * outputs. */
+int bacon_rk_autotune(bacon_ctx* ctx, const bacon_problem* problem,
+                      const bacon_rk_options* options, bacon_rk_result* result,
+                      int32_t* best_block, int32_t* best_blocks_per_sm);
+
 /* The same solve with the plain one-launch-per-attempt GPU baseline (state,
  * t and dt in HBM, host loop until every system is done).  Same results. */
 int bacon_rk_solve_plain(bacon_ctx* ctx, const bacon_problem* problem,
                          const bacon_rk_options* options,
                          bacon_rk_result* result);
+
+/* ---- BDF (src/ivp/bdf.rs) ------------------------------------------------ */
+typedef enum { BACON_BDF6 = 0, BACON_BDF2 = 1 } bacon_bdf_method;
+/* AS_COMPILED: the reference's BDFSolver::step (bdf.rs:495-634) with every
+ *   quirk of 0.16.2 kept (RK4 bootstrap, yield machine, f at t_n, the "+"
+ *   finite-difference Jacobian, Broyden updates of an explicit LU inverse, the
+ *   lower residual with the higher-order history weights, t -= dt - order on
+ *   a rejected bootstrap).  On the reference's own test problems it yields no
+ *   items; on Robertson it stops with MaximumIterationsExceeded.
+ * CORRECTED: the engine's stiff BDF: orders 1..6 ramped up implicitly, f at
+ *   t_{n+1}, Newton with the analytic Jacobian and partial-pivot LU, the
+ *   reference's error estimate ||y_q - y_{q-1}|| and dt control. */
+typedef enum { BACON_BDF_AS_COMPILED = 0, BACON_BDF_CORRECTED = 1 } bacon_bdf_mode;
+
+typedef struct {
+  int32_t method;         /* bacon_bdf_method */
+  int32_t mode;           /* bacon_bdf_mode */
+  int32_t memory;         /* bacon_memory */
+  int32_t max_iter;       /* corrector iterations; 0 = 1000 (as_compiled, the
+                             reference's bound, bdf.rs:449) or 8 (corrected) */
+  int64_t max_steps;      /* cap on step() calls per system, 0 = 10,000,000 */
+  int32_t block;          /* 0 = 128 */
+  int32_t blocks_per_sm;  /* 0 = occupancy model */
+} bacon_bdf_options;
+
+/* Batched BDF6 / BDF2 solve of systems with dim <= 8 (one system per
+ * thread).  Same result semantics as bacon_rk_solve (rejected = Redo count). */
+int bacon_bdf_solve(bacon_ctx* ctx, const bacon_problem* problem,
+                    const bacon_bdf_options* options, bacon_rk_result* result);
 
 /* ---- discrete adjoint ---------------------------------------------------- */
 /* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with

@@ -140,6 +140,10 @@ typedef struct {
   double tol, dt_min, dt_max;
 } oracle_bdf_cfg;
 
+/* Analytic Jacobian of a registry right-hand side, row-major dim x dim. */
+int oracle_rhs_jacobian(int32_t rhs, int32_t dim, double t, const double* y, const double* p,
+                        const double* shared, double* J);
+
 int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim,
                              const double* p, const double* shared, double t0,
                              double t_end, const double* y0, double* y_out,

@@ -237,3 +237,31 @@ def rk_fwdsens_one(cfg, rhs, y0, params, t0, t_end, target):
     st = L.oracle_rk_fwdsens_one(ctypes.byref(cfg), rhs, y0.shape[0], p.shape[0], _dp(p), t0, t_end,
                                  _dp(y0), _dp(tg), _dp(gy), _dp(gp))
     return st, gy, gp
+
+
+def bdf_cfg(method=BDF6, mode=BDF_CORRECTED, dyn_dim=False, max_iter=0, max_steps=0, tol=1e-6,
+            dt_min=1e-10, dt_max=1.0):
+    return _BdfCfg(method, mode, int(dyn_dim), int(max_iter), int(max_steps), tol, dt_min, dt_max)
+
+
+def bdf_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0) -> Path:
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    dim = y0.shape[0]
+    p = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    y = np.zeros(dim)
+    t = ctypes.c_double()
+    a = ctypes.c_int64()
+    r = ctypes.c_int64()
+    tt = ty = None
+    if traj_cap:
+        tt = np.zeros(traj_cap)
+        ty = np.zeros((traj_cap, dim))
+    st = L.oracle_bdf_solve_one(ctypes.byref(cfg), rhs, dim, _dp(p), _dp(sh), t0, t_end,
+                                _dp(y0), _dp(y), ctypes.byref(t), ctypes.byref(a),
+                                ctypes.byref(r), _dp(tt), _dp(ty), traj_cap)
+    if traj_cap:
+        n = min(a.value, traj_cap)
+        tt, ty = tt[:n], ty[:n]
+    return Path(st, t.value, y, a.value, r.value, tt, ty)

@@ -5,6 +5,7 @@
 
 #define ORC_MAX_STAGES 6
 #define ORC_MAX_DIM 512
+#define ORC_MAX_BDF_DIM 128
 
 typedef struct {
   int s;

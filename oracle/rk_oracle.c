@@ -410,3 +410,80 @@ double oracle_rk_solve_batch(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim,
   clock_gettime(CLOCK_MONOTONIC, &b);
   return (double)(b.tv_sec - a.tv_sec) + 1e-9 * (double)(b.tv_nsec - a.tv_nsec);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Analytic Jacobians J[r*dim + c] = d f_r / d y_c of the registry right-hand
+ * sides, in a fixed evaluation order (the CUDA engine mirrors it). */
+int oracle_rhs_jacobian(int32_t rhs, int32_t dim, double t, const double* y, const double* p,
+                        const double* shared, double* J) {
+  (void)t;
+  for (int i = 0; i < dim * dim; ++i) J[i] = 0.0;
+  switch (rhs) {
+    case ORC_RHS_EXP:
+      for (int d = 0; d < dim; ++d) J[d * dim + d] = 1.0;
+      return 0;
+    case ORC_RHS_DECAY:
+      for (int d = 0; d < dim; ++d) J[d * dim + d] = -1.0;
+      return 0;
+    case ORC_RHS_QUADRATIC:
+    case ORC_RHS_SINE:
+      return 0;
+    case ORC_RHS_HARMONIC:
+      J[1] = 1.0;
+      J[2] = -1.0;
+      return 0;
+    case ORC_RHS_VDP: {
+      const double mu = p[0];
+      J[1] = 1.0;
+      J[2] = (((-2.0 * mu) * y[0]) * y[1]) - 1.0;
+      J[3] = mu * (1.0 - (y[0] * y[0]));
+      return 0;
+    }
+    case ORC_RHS_LORENZ:
+      J[0] = -p[0];
+      J[1] = p[0];
+      J[3] = p[1] - y[2];
+      J[4] = -1.0;
+      J[5] = -y[0];
+      J[6] = y[1];
+      J[7] = y[0];
+      J[8] = -p[2];
+      return 0;
+    case ORC_RHS_LOTKA:
+      J[0] = p[0] - (p[1] * y[1]);
+      J[1] = -(p[1] * y[0]);
+      J[2] = p[2] * y[1];
+      J[3] = (p[2] * y[0]) - p[3];
+      return 0;
+    case ORC_RHS_ROBERTSON: {
+      const double k1 = p[0], k2 = p[1], k3 = p[2];
+      J[0] = -k1;
+      J[1] = k3 * y[2];
+      J[2] = k3 * y[1];
+      J[3] = k1;
+      J[4] = ((-2.0 * k2) * y[1]) - (k3 * y[2]);
+      J[5] = -(k3 * y[1]);
+      J[7] = (2.0 * k2) * y[1];
+      return 0;
+    }
+    case ORC_RHS_CHAIN: {
+      const int n = dim / 2;
+      const double c = p[n];
+      for (int i = 0; i < n; ++i) {
+        J[i * dim + n + i] = 1.0;
+        const double kl = p[i];
+        const double kr = (i + 1 < n) ? p[i + 1] : 0.0;
+        J[(n + i) * dim + i] = -(kl + kr);
+        if (i > 0) J[(n + i) * dim + i - 1] = kl;
+        if (i + 1 < n) J[(n + i) * dim + i + 1] = kr;
+        J[(n + i) * dim + n + i] = -c;
+      }
+      return 0;
+    }
+    case ORC_RHS_LINEAR:
+      for (int i = 0; i < dim * dim; ++i) J[i] = shared[i];
+      return 0;
+    default:
+      return -1;
+  }
+}

@@ -1,0 +1,53 @@
+"""Batched RKF45 on y' = A y with one shared A (the GEMM right-hand side).
+
+FP64_EXACT stage GEMMs sum every matvec in the CPU oracle's order, so the
+lock-step engine is bit-identical to the oracle's per-system solve; all
+modes are checked against the exact solution Q exp(-Lambda t) Q^T y0."""
+import numpy as np
+import pytest
+
+from bacon_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(E, b, precision=0, layout=2):
+    return E.rk_solve(b.y0, None, b.t0, b.t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                      layout=layout, precision=precision, shared=b.extra["A"])
+
+
+@pytest.mark.parametrize("dim", [64, 256])
+def test_linear_exact_matches_oracle(engine, oracle, dim):
+    b = W.linear_shared(n=96, dim=dim, seed=21)
+    sol = _solve(engine, b)
+    assert sol.code == 0
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+    ref = oracle.rk_solve_batch(cfg, b.rhs, b.y0, None, b.t0, b.t_end, shared=b.extra["A"])
+    np.testing.assert_array_equal(sol.accepted, ref["accepted"])
+    np.testing.assert_array_equal(sol.rejected, ref["rejected"])
+    np.testing.assert_array_equal(sol.t, ref["t"])
+    np.testing.assert_array_equal(sol.y, ref["y"])
+
+
+def test_linear_fma_close_to_exact_solution(engine):
+    b = W.linear_shared(n=512, dim=256, seed=22)
+    ex = b.extra["exact"](5.0)
+    for prec in (0, 1):
+        sol = _solve(engine, b, precision=prec)
+        assert (sol.status == 0).all()
+        assert np.abs(sol.y - ex).max() < 1e-7
+
+
+@pytest.mark.parametrize("dim", [128, 256])
+def test_linear_tensor_core_split(engine, dim):
+    """tcgen05 stage GEMM with 6 x 6-bit bf16 slices: the product A*Y is exact
+    to ~2^-36 relative, so the engine takes the FP64 engine's steps and
+    reaches the same accuracy against the exact solution."""
+    b = W.linear_shared(n=1024, dim=dim, seed=23)
+    ex = b.extra["exact"](5.0)
+    fp = _solve(engine, b, precision=0)
+    tc = _solve(engine, b, precision=engine.TC_SPLIT)
+    assert (tc.status == 0).all()
+    assert np.abs(tc.y - ex).max() < 1e-7
+    assert np.mean(tc.accepted == fp.accepted) >= 0.99
+    assert np.abs(tc.y - fp.y).max() < 1e-8
