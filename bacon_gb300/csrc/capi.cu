@@ -485,7 +485,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     ta.sy = c->tc_sy.as<__nv_bfloat16>();
     ta.ey = c->tc_ey.as<int32_t>();
     ta.error_flag = d_err;
-    BACON_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned int), c->stream));
+    BACON_CUDA(cudaMemsetAsync(c->d_ctl + 3, 0, sizeof(unsigned long long), c->stream));
     const double* Ap = A;
     __nv_bfloat16* sa = c->tc_sa.as<__nv_bfloat16>();
     int32_t* ea = c->tc_ea.as<int32_t>();
@@ -514,8 +514,12 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
     BACON_CUDA(cudaLaunchKernel(k.control, dim3(cg), dim3(256), cargs, 0, c->stream));
     BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    if (tc)  // a tensor-core stage that gave up a bounded wait ends the solve
+      BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 3, c->d_ctl + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 c->stream));
     BACON_CUDA(cudaStreamSynchronize(c->stream));
     c->launches += k.stages + 1;
+    if (tc && c->h_ctl[3] != 0) return fail(BACON_CUDA_ERROR, "tensor-core stage: a bounded mbarrier wait gave up");
   }
   BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
   c->ev_valid = true;

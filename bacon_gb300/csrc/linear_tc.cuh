@@ -81,8 +81,12 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                : "memory");
 }
 
+// Waits for the mbarrier phase with a time limit of about one second of SM
+// clock; on expiry it raises the error flag and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase, unsigned int* error_flag) {
-  for (long long it = 0; it < (1ll << 26); ++it) {
+  const long long start = clock64();
+  for (;;) {
+    if (clock64() - start > 2000000000ll) break;
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"

@@ -17,18 +17,28 @@
 
 namespace bacon {
 
-// log2 of a non-negative double over its whole range, to float accuracy: the
-// exponent from the bit pattern, the mantissa through the FP32 log2.  A step
-// factor needs no more, and no float over- or underflow can occur (tiny
-// end-clamped steps make (tol*dt)^2 far smaller than FLT_MIN).
-__device__ __forceinline__ float log2_wide(double x) {
-  if (!(x > 0.0)) return (x == 0.0) ? -INFINITY : __int_as_float(0x7fc00000);
-  if (__double2hiint(x) >= 0x7ff00000) return INFINITY;
-  const int hi = __double2hiint(x);
-  const int e = ((hi >> 20) & 0x7ff) - 1023;
-  const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, __double2loint(x));  // [1, 2)
-  return static_cast<float>(e) + __log2f(__double2float_rn(m));
+// log2(num / den) for num > 0 and den >= 0 over the whole double range, to
+// float accuracy near 1: the exponent difference as an integer plus log2 of
+// the ratio of the two mantissas (both in [1, 2), so the float quotient lies
+// in (1/2, 2) and neither over- nor underflows however small (tol*dt)^2 gets).
+// A zero den gives +inf, a NaN den NaN, an infinite den -inf.
+__device__ __forceinline__ float log2_ratio(double num, double den) {
+  if (!(den > 0.0)) return (den == 0.0) ? INFINITY : __int_as_float(0x7fc00000);
+  if (__double2hiint(den) >= 0x7ff00000) return -INFINITY;
+  if (!(num > 0.0)) return -INFINITY;
+  const int hn = __double2hiint(num), hd = __double2hiint(den);
+  const int e = ((hn >> 20) & 0x7ff) - ((hd >> 20) & 0x7ff);
+  const double mn = __hiloint2double((hn & 0x000fffff) | 0x3ff00000, __double2loint(num));
+  const double md = __hiloint2double((hd & 0x000fffff) | 0x3ff00000, __double2loint(den));
+  const float q = __fdiv_rn(__double2float_rn(mn), __double2float_rn(md));
+  return static_cast<float>(e) + log2f(q);
 }
+
+// Largest factor a rejected attempt may keep: 1 - 2^-20.  The reference's
+// factor (tol/err)^(1/4) is below 1 whenever err > tol; in FP32 a ratio
+// within ~1e-7 of 1 rounds to exactly 1, which would leave dt unchanged and
+// repeat the same rejected attempt until max_attempts.
+constexpr float kRejectMaxFactor = 0.99999905f;
 
 template <class Tab, class Rhs>
 __global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
@@ -160,9 +170,10 @@ __global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
         });
       }
 
-      // (tol/err)^(1/4) = (thr / n2)^(1/8) = 2^((log2 thr - log2 n2) / 8);
-      // +inf when the error vanishes, NaN for a NaN error (as the reference).
-      const float delta = exp2f(0.125f * (log2_wide(thr) - log2_wide(n2)));
+      // (tol/err)^(1/4) = (thr / n2)^(1/8) = 2^(log2(thr / n2) / 8); +inf
+      // when the error vanishes, NaN for a NaN error (as the reference).
+      float delta = exp2f(0.125f * log2_ratio(thr, n2));
+      if (!ok && delta > kRejectMaxFactor) delta = kRejectMaxFactor;
       if (delta <= 0.1f) dt = __dmul_rn(dt, 0.1);
       else if (delta >= 4.0f) dt = __dmul_rn(dt, 4.0);
       else dt = __dmul_rn(dt, static_cast<double>(delta));

@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--n", type=int, default=1 << 20, help="systems per GPU")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="systems in the CPU sample")
     ap.add_argument("--skip-extras", action="store_true", help="skip plain/FMA/CPU side measurements")
+    ap.add_argument("--precision", default="fp64_exact", choices=["fp64_exact", "fp64_fma", "fp32_comp"],
+                    help="arithmetic of the timed solve (the headline is fp64_exact)")
     return ap.parse_args()
 
 
@@ -56,7 +58,7 @@ def workload(n, rank):
 def config(args, b):
     return {"workload": "lorenz63", "n_systems_per_gpu": b.n, "dim": 3, "tol": b.tol,
             "dt_min": b.dt_min, "dt_max": b.dt_max, "t0": 0.0, "t_end": "U[1,20] per system",
-            "method": "RKF45", "tableau": "fehlberg", "precision": "fp64_exact",
+            "method": "RKF45", "tableau": "fehlberg", "precision": args.precision,
             "parity": "bit-identical to the CPU restatement (tests/test_rk_gpu.py)",
             "l2": "256 MiB device write before every timed step (inputs ~100 MB fit in L2)",
             "parallelism": f"replicas x{args.gpus} (independent batches, no collective)"}
@@ -148,6 +150,73 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def other_workloads(E, W, ctx, dev, torch):
+    """The other benchmark workloads, one timed solve each (device-resident)."""
+    out = {}
+
+    def to_dev(*xs):
+        return [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in xs]
+
+    # Van der Pol, 4096 systems, t in [0, 10] (the CPU-runnable workload).
+    vb = W.van_der_pol()
+    vy, vp = to_dev(vb.y0, vb.params)
+    kw = dict(rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, layout=E.FEHLBERG, ctx=ctx)
+    E.rk_solve(vy, vp, 0.0, 10.0, **kw)
+    s = E.rk_solve(vy, vp, 0.0, 10.0, **kw)
+    ms = ctx.last_kernel_ms()
+    out["van_der_pol_4096"] = {"value": vb.n / (ms * 1e-3), "unit": "solves/s", "kernel_ms": ms,
+                               "statuses_ok": bool((s.status == 0).all().item())}
+
+    # Linear y' = A y, shared A (n = 256), 65,536 states, tol 1e-8.
+    lb = W.linear_shared()
+    ly, lA = to_dev(lb.y0, lb.extra["A"])
+    lk = dict(rhs=lb.rhs, tol=lb.tol, dt_min=lb.dt_min, dt_max=lb.dt_max, layout=E.FEHLBERG, ctx=ctx, shared=lA)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tc = E.rk_solve(ly, None, 0.0, 5.0, precision=E.TC_SPLIT, **lk)
+    torch.cuda.synchronize()
+    tc_s = time.perf_counter() - t0
+    sub = 8192
+    sy_, = to_dev(lb.y0[:, :sub])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fp = E.rk_solve(sy_, None, 0.0, 5.0, precision=E.FP64_FMA, **lk)
+    torch.cuda.synchronize()
+    fp_s = time.perf_counter() - t0
+    exact = lb.extra["exact"](5.0, slice(0, sub))
+    out["linear_shared_A_256"] = {
+        "tensor_split": {"value": lb.n / tc_s, "unit": "solves/s", "n": lb.n,
+                         "max_abs_err_vs_exact_first_8192": float(np.abs(tc.y[:, :sub].cpu().numpy() - exact).max()),
+                         "statuses_ok": bool((tc.status == 0).all().item())},
+        "fp64_fma": {"value": sub / fp_s, "unit": "solves/s", "n": sub,
+                     "max_abs_err_vs_exact": float(np.abs(fp.y.cpu().numpy() - exact).max())},
+        "what": "lock-step RKF45 rounds; stage GEMM 256x256 x 256xN on tcgen05 (bf16 6x6-bit slices, exact FP32 "
+                "accumulation) vs FP64 DFMA SIMT GEMM; wall time of the whole solve"}
+
+    # Stiff batch: Robertson kinetics and spring-mass chains, corrected BDF6.
+    rb = W.robertson()
+    ry, rp = to_dev(rb.y0, rb.params)
+    rk = dict(rhs=rb.rhs, tol=rb.tol, dt_min=rb.dt_min, dt_max=rb.dt_max, ctx=ctx)
+    E.bdf_solve(ry, rp, 0.0, 1e4, **rk)
+    rs = E.bdf_solve(ry, rp, 0.0, 1e4, **rk)
+    rob_ms = ctx.last_kernel_ms()
+    chains = {}
+    for m in (2, 3, 4):
+        cb = W.spring_chains(n=rb.n // 3, masses=m)
+        cy, cp = to_dev(cb.y0, cb.params)
+        ck = dict(rhs=cb.rhs, tol=cb.tol, dt_min=cb.dt_min, dt_max=cb.dt_max, ctx=ctx)
+        E.bdf_solve(cy, cp, 0.0, 10.0, **ck)
+        cs = E.bdf_solve(cy, cp, 0.0, 10.0, **ck)
+        chains[f"{m}_masses"] = {"value": cb.n / (ctx.last_kernel_ms() * 1e-3), "unit": "solves/s", "n": cb.n,
+                                 "statuses_ok": bool((cs.status == 0).all().item())}
+    out["bdf6_stiff"] = {"robertson": {"value": rb.n / (rob_ms * 1e-3), "unit": "solves/s", "n": rb.n,
+                                       "t_end": 1e4, "statuses_ok": bool((rs.status == 0).all().item())},
+                         "spring_chains": chains,
+                         "what": "corrected BDF6 (Newton, analytic Jacobian, partial-pivot LU), one system per "
+                                 "thread; chains with more than 4 masses are not on the GPU yet"}
+    return out
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -178,7 +247,9 @@ def main():
     out = E.alloc_outputs(3, b.n, device=True)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    def solve(precision=E.FP64_EXACT, dst=None):
+    prec = {"fp64_exact": E.FP64_EXACT, "fp64_fma": E.FP64_FMA, "fp32_comp": E.FP32_COMP}[args.precision]
+
+    def solve(precision=prec, dst=None):
         return E.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
                           layout=E.FEHLBERG, precision=precision, out=dst or out, ctx=ctx,
                           raise_on_error=True)
@@ -240,7 +311,7 @@ def main():
     h2d = hy0.nbytes + hprm.nbytes + ht0.nbytes + hte.nbytes
     d2h = sum(hout[k].nbytes for k in ("y", "t", "accepted", "rejected", "status"))
     E.rk_solve(hy0, hprm, ht0, hte, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
-               layout=E.FEHLBERG, out=hout, ctx=ctx, raise_on_error=True)
+               layout=E.FEHLBERG, precision=prec, out=hout, ctx=ctx, raise_on_error=True)
     barrier()
     e2e_s = []
     for _ in range(args.steps):
@@ -248,7 +319,7 @@ def main():
         torch.cuda.synchronize()
         s0 = time.perf_counter()
         E.rk_solve(hy0, hprm, ht0, hte, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
-                   layout=E.FEHLBERG, out=hout, ctx=ctx, raise_on_error=True)
+                   layout=E.FEHLBERG, precision=prec, out=hout, ctx=ctx, raise_on_error=True)
         e2e_s.append(time.perf_counter() - s0)
     e2e_total = sum(e2e_s)
     if world > 1:
@@ -344,6 +415,7 @@ def main():
             "e2e_value": lv.n / adj_wall, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
             "record_forward_ms": rec_ms, "reverse_ms": rev_ms, "cost_vs_forward": adj_ms / fwd_ms,
             "max_rel_diff_vs_frozen_central_fd_h1e-6": fd_rel, "fd_sample": 16}
+        extras.update(other_workloads(E, W, ctx, dev, torch))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
