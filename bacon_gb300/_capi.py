@@ -98,6 +98,35 @@ class BdfOptions(ctypes.Structure):
     ]
 
 
+class RaggedProblem(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int64),
+        ("rhs", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("y_offsets", ctypes.c_void_p),
+        ("p_offsets", ctypes.c_void_p),
+        ("y0", ctypes.c_void_p),
+        ("params", ctypes.c_void_p),
+        ("t0", ctypes.c_void_p),
+        ("t_end", ctypes.c_void_p),
+        ("t0_scalar", ctypes.c_double),
+        ("t_end_scalar", ctypes.c_double),
+        ("tol", ctypes.c_double),
+        ("dt_min", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+    ]
+
+
+class RaggedResult(ctypes.Structure):
+    _fields_ = [
+        ("y_final", ctypes.c_void_p),
+        ("t_final", ctypes.c_void_p),
+        ("accepted", ctypes.c_void_p),
+        ("rejected", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+    ]
+
+
 class Adjoint(ctypes.Structure):
     _fields_ = [
         ("target", ctypes.c_void_p),
@@ -125,6 +154,10 @@ SIGNATURES = {
     "bacon_rk_validate": (ctypes.c_int, [ctypes.POINTER(Problem)]),
     "bacon_bdf_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(BdfOptions),
                                        ctypes.POINTER(RkResult)]),
+    "bacon_ragged_validate": (ctypes.c_int, [ctypes.POINTER(RaggedProblem)]),
+    "bacon_bdf_solve_mixed": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RaggedProblem),
+                                             ctypes.POINTER(BdfOptions), ctypes.POINTER(RkResult),
+                                             ctypes.POINTER(RaggedResult)]),
     "bacon_rk_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                          ctypes.POINTER(RkResult), I32P, I32P]),
     "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),

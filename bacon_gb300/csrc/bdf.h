@@ -14,6 +14,11 @@ struct BdfEntry {
 };
 
 void register_bdf_corrected(std::vector<BdfEntry>& v);
+
+// Mixed stiff-batch kernel __global__ void(BdfArgs, int small_dyn, RaggedArgs)
+// for a uniform part of (small_rhs, small_dim), or for none (small_rhs < 0);
+// null when not compiled.
+const void* bdf_mixed_kernel_for(int small_rhs, int small_dim);
 void register_bdf_as_compiled(std::vector<BdfEntry>& v);
 
 inline std::vector<BdfEntry> all_bdf_kernels() {

@@ -210,19 +210,149 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
   return false;
 }
 
+// One system of the corrected BDF, integrated by the calling thread alone
+// (state in registers and local memory).
 template <class Rhs>
-__global__ void __launch_bounds__(128) bdf_corrected_kernel(const BdfArgs a, int dyn_dim) {
+__device__ __forceinline__ void bdf_corrected_system(const BdfArgs& a, int64_t idx, bool dyn) {
   using O = ExactOps;
   constexpr int D = Rhs::DIM;
   constexpr int P = Rhs::NP > 0 ? Rhs::NP : 1;
   const int64_t n = a.n;
-  const bool dyn = dyn_dim != 0;
   double dt_min = a.dt_min;
   const double dt_max = a.dt_max;
   if (dt_min > dt_max) dt_min = dt_max;
   const int qmax = a.qmax;
-  const unsigned lane = threadIdx.x & 31u;
+  double p[P];
+#pragma unroll
+  for (int k = 0; k < Rhs::NP; ++k) p[k] = a.params[k * n + idx];
+  double H[7][D], Hn[7][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) H[0][d] = a.y0[d * n + idx];
+  double t = a.t0 ? a.t0[idx] : a.t0_s;
+  const double t_end = a.t_end ? a.t_end[idx] : a.t_end_s;
+  double dt = O::mul(O::add(dt_max, dt_min), 0.5);
+  int k = 1;
+  int32_t acc = 0, rej = 0, status = kStOk;
+  double last_t = t, last_y[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) last_y[d] = H[0][d];
+  int64_t steps = 0;
+  if (t >= t_end) status = kStTimeEndOob;
+  while (status == kStOk && t < t_end) {
+    if (steps >= a.max_steps) {
+      status = kStMaxAttempts;
+      break;
+    }
+    ++steps;
+    double h = dt;
+    if (O::add(t, h) >= t_end) h = O::sub(t_end, t);
+    const int q = (k < qmax) ? k : qmax;
+    double w[7];
+    double HH[7][D];
+    if (h != dt && k > 1) {
+      const double ratio = O::div(h, dt);
+      for (int j = 0; j < k; ++j) {
+        lagrange_weights(k - 1, O::mul(-ratio, static_cast<double>(j)), w);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double s = 0.0;
+          for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], H[i][d]));
+          HH[j][d] = s;
+        }
+      }
+    } else {
+      for (int j = 0; j < k; ++j)
+#pragma unroll
+        for (int d = 0; d < D; ++d) HH[j][d] = H[j][d];
+    }
+    double pred[D], yh[D], yl[D], diff[D];
+    lagrange_weights(k - 1, 1.0, w);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double s = 0.0;
+      for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], HH[i][d]));
+      pred[d] = s;
+    }
+    const double t1 = O::add(t, h);
+    bool ok = bdf_newton<Rhs, D>(p, t1, h, q, HH, pred, yh, a.max_iter, a.tol);
+    double error;
+    if (ok && q >= 2) {
+      ok = bdf_newton<Rhs, D>(p, t1, h, q - 1, HH, yh, yl, a.max_iter, a.tol);
+#pragma unroll
+      for (int d = 0; d < D; ++d) diff[d] = O::sub(yh[d], yl[d]);
+      error = bdf_norm(diff, dyn);
+    } else {
+      double f0[D];
+      Rhs::template eval<O>(t, H[0], p, f0);
+#pragma unroll
+      for (int d = 0; d < D; ++d) diff[d] = O::mul(0.5, O::sub(yh[d], O::add(H[0][d], O::mul(h, f0[d]))));
+      error = bdf_norm(diff, dyn);
+    }
+    if (ok && error <= a.tol) {
+      const int kk = (k < 7) ? k + 1 : 7;
+      for (int i = kk - 1; i >= 1; --i)
+#pragma unroll
+        for (int d = 0; d < D; ++d) H[i][d] = H[i - 1][d];
+#pragma unroll
+      for (int d = 0; d < D; ++d) H[0][d] = yh[d];
+      k = kk;
+      t = t1;
+      if (a.traj_t != nullptr && acc < a.traj_cap) {
+        const int64_t slot = idx * a.traj_cap + acc;
+        a.traj_t[slot] = t;
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = yh[d];
+      }
+      ++acc;
+      last_t = t;
+#pragma unroll
+      for (int d = 0; d < D; ++d) last_y[d] = yh[d];
+      if (h != dt) continue;
+      if (error < O::mul(0.1, a.tol) && k == qmax + 1 && O::mul(dt, 2.0) <= dt_max) {
+        const int nk = (k + 1) / 2;
+        for (int i = 1; i < nk; ++i)
+#pragma unroll
+          for (int d = 0; d < D; ++d) H[i][d] = H[2 * i][d];
+        k = nk;
+        dt = O::mul(dt, 2.0);
+      }
+      continue;
+    }
+    ++rej;
+    const double nd = O::mul(dt, 0.5);
+    if (nd < dt_min) {
+      status = kStMinDt;
+      break;
+    }
+    if (k > 1) {
+      for (int j = 0; j < k; ++j) {
+        lagrange_weights(k - 1, O::mul(-0.5, static_cast<double>(j)), w);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double s = 0.0;
+          for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], H[i][d]));
+          Hn[j][d] = s;
+        }
+      }
+      for (int j = 0; j < k; ++j)
+#pragma unroll
+        for (int d = 0; d < D; ++d) H[j][d] = Hn[j][d];
+    }
+    dt = nd;
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) a.y_out[d * n + idx] = last_y[d];
+  a.t_out[idx] = last_t;
+  a.accepted[idx] = acc;
+  a.rejected[idx] = rej;
+  a.status[idx] = status;
+  if (status != kStOk) atomicMin(a.first_fail, static_cast<unsigned long long>(idx));
+}
 
+// Every thread pulls systems from the work counter until the batch is done.
+template <class Rhs>
+__device__ __forceinline__ void bdf_corrected_thread_loop(const BdfArgs& a, bool dyn) {
+  const unsigned lane = threadIdx.x & 31u;
   for (;;) {
     unsigned long long ticket = 0;
     const unsigned mask = __activemask();
@@ -230,134 +360,14 @@ __global__ void __launch_bounds__(128) bdf_corrected_kernel(const BdfArgs a, int
     if (static_cast<int>(lane) == leader) ticket = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(mask)));
     ticket = __shfl_sync(mask, ticket, leader) + __popc(mask & ((1u << lane) - 1u));
     const int64_t idx = static_cast<int64_t>(ticket);
-    if (idx >= n) break;
-
-    double p[P];
-#pragma unroll
-    for (int k = 0; k < Rhs::NP; ++k) p[k] = a.params[k * n + idx];
-    double H[7][D], Hn[7][D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) H[0][d] = a.y0[d * n + idx];
-    double t = a.t0 ? a.t0[idx] : a.t0_s;
-    const double t_end = a.t_end ? a.t_end[idx] : a.t_end_s;
-    double dt = O::mul(O::add(dt_max, dt_min), 0.5);
-    int k = 1;
-    int32_t acc = 0, rej = 0, status = kStOk;
-    double last_t = t, last_y[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) last_y[d] = H[0][d];
-    int64_t steps = 0;
-    if (t >= t_end) status = kStTimeEndOob;
-    while (status == kStOk && t < t_end) {
-      if (steps >= a.max_steps) {
-        status = kStMaxAttempts;
-        break;
-      }
-      ++steps;
-      double h = dt;
-      if (O::add(t, h) >= t_end) h = O::sub(t_end, t);
-      const int q = (k < qmax) ? k : qmax;
-      double w[7];
-      double HH[7][D];
-      if (h != dt && k > 1) {
-        const double ratio = O::div(h, dt);
-        for (int j = 0; j < k; ++j) {
-          lagrange_weights(k - 1, O::mul(-ratio, static_cast<double>(j)), w);
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            double s = 0.0;
-            for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], H[i][d]));
-            HH[j][d] = s;
-          }
-        }
-      } else {
-        for (int j = 0; j < k; ++j)
-#pragma unroll
-          for (int d = 0; d < D; ++d) HH[j][d] = H[j][d];
-      }
-      double pred[D], yh[D], yl[D], diff[D];
-      lagrange_weights(k - 1, 1.0, w);
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        double s = 0.0;
-        for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], HH[i][d]));
-        pred[d] = s;
-      }
-      const double t1 = O::add(t, h);
-      bool ok = bdf_newton<Rhs, D>(p, t1, h, q, HH, pred, yh, a.max_iter, a.tol);
-      double error;
-      if (ok && q >= 2) {
-        ok = bdf_newton<Rhs, D>(p, t1, h, q - 1, HH, yh, yl, a.max_iter, a.tol);
-#pragma unroll
-        for (int d = 0; d < D; ++d) diff[d] = O::sub(yh[d], yl[d]);
-        error = bdf_norm(diff, dyn);
-      } else {
-        double f0[D];
-        Rhs::template eval<O>(t, H[0], p, f0);
-#pragma unroll
-        for (int d = 0; d < D; ++d) diff[d] = O::mul(0.5, O::sub(yh[d], O::add(H[0][d], O::mul(h, f0[d]))));
-        error = bdf_norm(diff, dyn);
-      }
-      if (ok && error <= a.tol) {
-        const int kk = (k < 7) ? k + 1 : 7;
-        for (int i = kk - 1; i >= 1; --i)
-#pragma unroll
-          for (int d = 0; d < D; ++d) H[i][d] = H[i - 1][d];
-#pragma unroll
-        for (int d = 0; d < D; ++d) H[0][d] = yh[d];
-        k = kk;
-        t = t1;
-        if (a.traj_t != nullptr && acc < a.traj_cap) {
-          const int64_t slot = idx * a.traj_cap + acc;
-          a.traj_t[slot] = t;
-#pragma unroll
-          for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = yh[d];
-        }
-        ++acc;
-        last_t = t;
-#pragma unroll
-        for (int d = 0; d < D; ++d) last_y[d] = yh[d];
-        if (h != dt) continue;
-        if (error < O::mul(0.1, a.tol) && k == qmax + 1 && O::mul(dt, 2.0) <= dt_max) {
-          const int nk = (k + 1) / 2;
-          for (int i = 1; i < nk; ++i)
-#pragma unroll
-            for (int d = 0; d < D; ++d) H[i][d] = H[2 * i][d];
-          k = nk;
-          dt = O::mul(dt, 2.0);
-        }
-        continue;
-      }
-      ++rej;
-      const double nd = O::mul(dt, 0.5);
-      if (nd < dt_min) {
-        status = kStMinDt;
-        break;
-      }
-      if (k > 1) {
-        for (int j = 0; j < k; ++j) {
-          lagrange_weights(k - 1, O::mul(-0.5, static_cast<double>(j)), w);
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            double s = 0.0;
-            for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], H[i][d]));
-            Hn[j][d] = s;
-          }
-        }
-        for (int j = 0; j < k; ++j)
-#pragma unroll
-          for (int d = 0; d < D; ++d) H[j][d] = Hn[j][d];
-      }
-      dt = nd;
-    }
-#pragma unroll
-    for (int d = 0; d < D; ++d) a.y_out[d * n + idx] = last_y[d];
-    a.t_out[idx] = last_t;
-    a.accepted[idx] = acc;
-    a.rejected[idx] = rej;
-    a.status[idx] = status;
-    if (status != kStOk) atomicMin(a.first_fail, static_cast<unsigned long long>(idx));
+    if (idx >= a.n) break;
+    bdf_corrected_system<Rhs>(a, idx, dyn);
   }
+}
+
+template <class Rhs>
+__global__ void __launch_bounds__(128) bdf_corrected_kernel(const BdfArgs a, int dyn_dim) {
+  bdf_corrected_thread_loop<Rhs>(a, dyn_dim != 0);
 }
 
 // ---------------------------------------------------------------------------

@@ -6,6 +6,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -17,6 +18,7 @@
 #include "linear.h"
 #include "linear_tc.cuh"
 #include "bdf_kernel.cuh"
+#include "bdf_ragged.cuh"
 #include "order.h"
 #include "plain.h"
 #include "registry.h"
@@ -107,7 +109,9 @@ struct bacon_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 0;
-  unsigned long long* d_ctl = nullptr;  // [0] work counter [1] first failing index [2] live
+  // [0] work counter [1] first failing index [2] live [3] adjoint queue /
+  // tensor-core error flag [4] ragged work counter [5] first failing ragged index
+  unsigned long long* d_ctl = nullptr;
   unsigned long long* h_ctl = nullptr;  // pinned mirror
   std::vector<bacon::RkEntry> kernels;
   DevBuf in_y0, in_params, in_t0, in_tend, out_y, out_t, out_acc, out_rej, out_st, out_tt, out_ty;
@@ -128,6 +132,8 @@ struct bacon_ctx {
   DevBuf adj_dt, adj_ck, adj_tgt, adj_loss, adj_gy, adj_gp;
   DevBuf lin_A, lin_y, lin_K, lin_t, lin_dt, lin_end, lin_att;
   DevBuf tc_sa, tc_ea, tc_sy, tc_ey;
+  DevBuf rg_yoff, rg_poff, rg_y0, rg_p, rg_t0, rg_te, rg_yout, rg_tout, rg_acc, rg_rej, rg_st, rg_ord, rg_lu,
+      rg_perm;
 };
 
 extern "C" {
@@ -145,8 +151,8 @@ int bacon_ctx_create(int device, bacon_ctx** out) {
   c->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&c->d_ctl), 4 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->h_ctl), 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&c->d_ctl), 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->h_ctl), 8 * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     delete c;
     return fail(BACON_CUDA_ERROR, std::string("bacon_ctx_create: ") + cudaGetErrorString(e));
@@ -873,6 +879,262 @@ extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon
   BACON_CUDA(cudaStreamSynchronize(c->stream));
   BACON_CUDA(cudaGetLastError());
   return batch_return_code(c, r, host, o);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed stiff batch: ragged systems (a warp each) and a uniform batch of
+// small systems (a thread each) in one launch of bdf_mixed_kernel.
+namespace {
+
+int validate_ragged(const bacon_ragged_problem* g, const std::vector<int64_t>& yo, const std::vector<int64_t>& po,
+                    int& max_dim) {
+  if (g->rhs != BACON_RHS_CHAIN) return fail(BACON_UNSUPPORTED, "ragged batches support rhs CHAIN");
+  if (!(g->tol > 0.0)) return fail(BACON_INVALID_ARGUMENT, "ragged tol must be > 0");
+  if (!(g->dt_min > 0.0) || !(g->dt_max > 0.0)) return fail(BACON_INVALID_ARGUMENT, "ragged dt bounds must be > 0");
+  if (yo[0] != 0 || po[0] != 0) return fail(BACON_INVALID_ARGUMENT, "ragged offsets must start at 0");
+  max_dim = 0;
+  for (int64_t i = 0; i < g->n; ++i) {
+    const int64_t d = yo[i + 1] - yo[i];
+    if (d < 2 || d > bacon::kRagMaxDim || d % 2 != 0)
+      return fail(BACON_INVALID_ARGUMENT, "ragged system " + std::to_string(i) + ": dim must be even, 2..128");
+    if (po[i + 1] - po[i] != d / 2 + 1)
+      return fail(BACON_INVALID_ARGUMENT, "ragged system " + std::to_string(i) + ": chain takes dim/2 + 1 params");
+    if (d > max_dim) max_dim = static_cast<int>(d);
+  }
+  return BACON_OK;
+}
+
+}  // namespace
+
+extern "C" int bacon_ragged_validate(const bacon_ragged_problem* g) {
+  if (!g) return fail(BACON_INVALID_ARGUMENT, "ragged problem is NULL");
+  if (g->n < 0) return fail(BACON_INVALID_ARGUMENT, "ragged n < 0");
+  if (g->n == 0) return BACON_OK;
+  if (!g->y_offsets || !g->p_offsets) return fail(BACON_INVALID_ARGUMENT, "ragged offsets are NULL");
+  std::vector<int64_t> yo(g->y_offsets, g->y_offsets + g->n + 1), po(g->p_offsets, g->p_offsets + g->n + 1);
+  int ld = 0;
+  return validate_ragged(g, yo, po, ld);
+}
+
+extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, const bacon_ragged_problem* g,
+                                     const bacon_bdf_options* opt, bacon_rk_result* ur, bacon_ragged_result* gr) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  if (!up && !g) return fail(BACON_INVALID_ARGUMENT, "both parts are NULL");
+  if (opt->method != BACON_BDF6 && opt->method != BACON_BDF2) return fail(BACON_INVALID_ARGUMENT, "unknown method");
+  if (opt->mode != BACON_BDF_CORRECTED) return fail(BACON_UNSUPPORTED, "the mixed batch runs the corrected BDF");
+  const bool host = opt->memory == BACON_MEM_HOST;
+  int rc;
+  if (up) {
+    if ((rc = bacon_rk_validate(up)) != BACON_OK) return rc;
+    if ((rc = check_result_ptrs(up, ur)) != BACON_OK) return rc;
+    if (ur->traj_t) return fail(BACON_UNSUPPORTED, "the mixed batch records no trajectory");
+  }
+  if (g && g->n < 0) return fail(BACON_INVALID_ARGUMENT, "ragged n < 0");
+  const int64_t gn = g ? g->n : 0;
+  if (gn > 0) {
+    if (!gr || !gr->y_final || !gr->t_final || !gr->accepted || !gr->rejected || !gr->status)
+      return fail(BACON_INVALID_ARGUMENT, "ragged result array is NULL");
+    if (!g->y_offsets || !g->p_offsets || !g->y0 || !g->params)
+      return fail(BACON_INVALID_ARGUMENT, "ragged input array is NULL");
+    if (gn >= (int64_t(1) << 32)) return fail(BACON_INVALID_ARGUMENT, "ragged n must be < 2^32");
+  }
+  const void* fn = bacon::bdf_mixed_kernel_for(up && up->n > 0 ? up->rhs : -1, up ? up->dim : 0);
+  if (!fn) return fail(BACON_UNSUPPORTED, "no mixed kernel for this uniform (rhs, dim): ROBERTSON or VDP");
+  const int64_t un = up ? up->n : 0;
+
+  // ragged offsets on the host: validation, the largest dimension, the order
+  std::vector<int64_t> yo, po;
+  int ld = 2;
+  if (gn > 0) {
+    yo.resize(gn + 1);
+    po.resize(gn + 1);
+    if (host) {
+      std::memcpy(yo.data(), g->y_offsets, (gn + 1) * sizeof(int64_t));
+      std::memcpy(po.data(), g->p_offsets, (gn + 1) * sizeof(int64_t));
+    } else {
+      BACON_CUDA(cudaSetDevice(c->device));
+      BACON_CUDA(cudaMemcpy(yo.data(), g->y_offsets, (gn + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+      BACON_CUDA(cudaMemcpy(po.data(), g->p_offsets, (gn + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    }
+    if ((rc = validate_ragged(g, yo, po, ld)) != BACON_OK) return rc;
+  }
+  if (un == 0 && gn == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  std::vector<uint32_t> order(gn);
+  for (int64_t i = 0; i < gn; ++i) order[i] = static_cast<uint32_t>(i);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return yo[a + 1] - yo[a] > yo[b + 1] - yo[b]; });
+
+  // launch shape
+  const int block = 128;
+  const int warps = block / 32;
+  const size_t smem = gn > 0 ? static_cast<size_t>(warps) * bacon::rag_smem_doubles(ld) * sizeof(double) : 0;
+  BACON_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  int max_bps = 0;
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, smem));
+  if (max_bps < 1) return fail(BACON_CUDA_ERROR, "mixed kernel cannot be resident");
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
+  if (bps > max_bps) bps = max_bps;
+  long long grid = static_cast<long long>(c->num_sms) * bps;
+  const long long need = gn + (un + block - 1) / block;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+
+  // uniform part
+  Resolved uo{};
+  bacon::BdfArgs a{};
+  int dyn = 0;
+  if (un > 0) {
+    if ((rc = stage_inputs(c, up, ur, host, uo)) != BACON_OK) return rc;
+    a.n = un;
+    a.y0 = uo.y0;
+    a.params = uo.params;
+    a.t0 = uo.t0;
+    a.t_end = uo.t_end;
+    a.t0_s = up->t0_scalar;
+    a.t_end_s = up->t_end_scalar;
+    a.tol = up->tol;
+    a.dt_min = up->dt_min;
+    a.dt_max = up->dt_max;
+    a.y_out = uo.y_out;
+    a.t_out = uo.t_out;
+    a.accepted = uo.acc;
+    a.rejected = uo.rej;
+    a.status = uo.st;
+    dyn = up->dyn_dim ? 1 : 0;
+  }
+  a.max_steps = opt->max_steps > 0 ? opt->max_steps : 10000000;
+  a.max_iter = opt->max_iter > 0 ? opt->max_iter : 8;
+  a.qmax = (opt->method == BACON_BDF6) ? 6 : 2;
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+
+  // ragged part
+  bacon::RaggedArgs rg{};
+  rg.n = gn;
+  rg.max_steps = a.max_steps;
+  rg.max_iter = a.max_iter;
+  rg.qmax = a.qmax;
+  rg.queue = c->d_ctl + 4;
+  rg.first_fail = c->d_ctl + 5;
+  rg.ld = ld;
+  const size_t ytot = gn > 0 ? static_cast<size_t>(yo[gn]) : 0;
+  const size_t ptot = gn > 0 ? static_cast<size_t>(po[gn]) : 0;
+  if (gn > 0) {
+    rg.t0_s = g->t0_scalar;
+    rg.t_end_s = g->t_end_scalar;
+    rg.tol = g->tol;
+    rg.dt_min = g->dt_min;
+    rg.dt_max = g->dt_max;
+    const size_t nn = static_cast<size_t>(gn);
+    BACON_CUDA(c->rg_ord.ensure(nn * sizeof(uint32_t)));
+    rg.order = c->rg_ord.as<uint32_t>();
+    const size_t slots = static_cast<size_t>(grid) * warps;
+    BACON_CUDA(c->rg_lu.ensure(slots * 2 * ld * ld * sizeof(double)));
+    BACON_CUDA(c->rg_perm.ensure(slots * 2 * ld * sizeof(int32_t)));
+    rg.lu = c->rg_lu.as<double>();
+    rg.perm = c->rg_perm.as<int32_t>();
+    if (host) {
+      BACON_CUDA(c->rg_yoff.ensure((nn + 1) * sizeof(int64_t)));
+      BACON_CUDA(c->rg_poff.ensure((nn + 1) * sizeof(int64_t)));
+      BACON_CUDA(c->rg_y0.ensure(ytot * sizeof(double)));
+      BACON_CUDA(c->rg_p.ensure(ptot * sizeof(double)));
+      BACON_CUDA(c->rg_yout.ensure(ytot * sizeof(double)));
+      BACON_CUDA(c->rg_tout.ensure(nn * sizeof(double)));
+      BACON_CUDA(c->rg_acc.ensure(nn * sizeof(int32_t)));
+      BACON_CUDA(c->rg_rej.ensure(nn * sizeof(int32_t)));
+      BACON_CUDA(c->rg_st.ensure(nn * sizeof(int32_t)));
+      rg.y_off = c->rg_yoff.as<int64_t>();
+      rg.p_off = c->rg_poff.as<int64_t>();
+      rg.y0 = c->rg_y0.as<double>();
+      rg.params = c->rg_p.as<double>();
+      rg.t0 = nullptr;
+      rg.t_end = nullptr;
+      if (g->t0) {
+        BACON_CUDA(c->rg_t0.ensure(nn * sizeof(double)));
+        rg.t0 = c->rg_t0.as<double>();
+      }
+      if (g->t_end) {
+        BACON_CUDA(c->rg_te.ensure(nn * sizeof(double)));
+        rg.t_end = c->rg_te.as<double>();
+      }
+      rg.y_out = c->rg_yout.as<double>();
+      rg.t_out = c->rg_tout.as<double>();
+      rg.accepted = c->rg_acc.as<int32_t>();
+      rg.rejected = c->rg_rej.as<int32_t>();
+      rg.status = c->rg_st.as<int32_t>();
+    } else {
+      rg.y_off = g->y_offsets;
+      rg.p_off = g->p_offsets;
+      rg.y0 = g->y0;
+      rg.params = g->params;
+      rg.t0 = g->t0;
+      rg.t_end = g->t_end;
+      rg.y_out = gr->y_final;
+      rg.t_out = gr->t_final;
+      rg.accepted = gr->accepted;
+      rg.rejected = gr->rejected;
+      rg.status = gr->status;
+    }
+  }
+
+  // copies in, counters, the launch, copies out
+  if (host && un > 0 && (rc = enqueue_h2d(c, up, uo)) != BACON_OK) return rc;
+  if (gn > 0) {
+    const size_t nn = static_cast<size_t>(gn);
+    BACON_CUDA(cudaMemcpyAsync(const_cast<uint32_t*>(rg.order), order.data(), nn * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, c->stream));
+    if (host) {
+      BACON_CUDA(cudaMemcpyAsync(const_cast<int64_t*>(rg.y_off), yo.data(), (nn + 1) * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, c->stream));
+      BACON_CUDA(cudaMemcpyAsync(const_cast<int64_t*>(rg.p_off), po.data(), (nn + 1) * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, c->stream));
+      BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(rg.y0), g->y0, ytot * sizeof(double), cudaMemcpyHostToDevice,
+                                 c->stream));
+      BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(rg.params), g->params, ptot * sizeof(double),
+                                 cudaMemcpyHostToDevice, c->stream));
+      if (rg.t0)
+        BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(rg.t0), g->t0, nn * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->stream));
+      if (rg.t_end)
+        BACON_CUDA(cudaMemcpyAsync(const_cast<double*>(rg.t_end), g->t_end, nn * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+    }
+  }
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 4, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 5, 0xff, sizeof(unsigned long long), c->stream));
+  void* args[] = {&a, &dyn, &rg};
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, smem, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  if (host && un > 0 && (rc = enqueue_d2h(c, up, ur, uo)) != BACON_OK) return rc;
+  if (host && gn > 0) {
+    const size_t nn = static_cast<size_t>(gn);
+    BACON_CUDA(cudaMemcpyAsync(gr->y_final, rg.y_out, ytot * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(gr->t_final, rg.t_out, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(gr->accepted, rg.accepted, nn * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(gr->rejected, rg.rejected, nn * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(gr->status, rg.status, nn * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  }
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 5, c->d_ctl + 5, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+  c->launches += 1;
+  c->ev_valid = true;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  const unsigned long long gf = c->h_ctl[5];
+  if (gn > 0 && gf != ~0ull) {
+    int32_t st = 0;
+    if (host) st = gr->status[gf];
+    else BACON_CUDA(cudaMemcpy(&st, rg.status + gf, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return fail(st, "ragged system " + std::to_string(gf) + " ended with status " + std::to_string(st));
+  }
+  if (un > 0) return batch_return_code(c, ur, host, uo);
+  return BACON_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int f
   const int64_t n = a.n;
   double t = a.t[sys], dt = a.dt[sys];
   const double end = a.end[sys];
+  auto att = a.attempts[sys];
   int32_t st = kLinRunning;
 
   if (!first) {
@@ -199,13 +200,19 @@ __global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int f
       if (lane == 0) a.accepted[sys] += 1;
     } else {
       if (lane == 0) a.rejected[sys] += 1;
+      // dt bitwise unchanged by a rejection: the next attempt is this one
+      // again, up to the cap (as in rk_persistent_kernel); jump there.
+      if (ndt == dt) {
+        if (lane == 0) a.rejected[sys] += static_cast<int32_t>(a.max_attempts - att);
+        att = a.max_attempts;
+      }
     }
     dt = ndt;
   }
   if (st == kLinRunning) {
     if (t >= end) {
-      st = (first && a.attempts[sys] == 0) ? kStTimeEndOob : kStOk;
-    } else if (a.attempts[sys] >= a.max_attempts) {
+      st = (first && att == 0) ? kStTimeEndOob : kStOk;
+    } else if (att >= a.max_attempts) {
       st = kStMaxAttempts;
     } else {
       if (Ops::add(t, dt) >= end) dt = Ops::sub(end, t);
@@ -216,8 +223,9 @@ __global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int f
     a.dt[sys] = dt;
     if (st != kLinRunning) {
       a.status[sys] = st;
+      a.attempts[sys] = att;
     } else {
-      a.attempts[sys] += 1;
+      a.attempts[sys] = att + 1;
       atomicAdd(a.live, 1u);
     }
   }

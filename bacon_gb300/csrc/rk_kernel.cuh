@@ -162,7 +162,6 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
       ++attempts;
       if (Ops::add(t, dt) >= end) dt = Ops::sub(end, t);  // rk.rs:366-368
       const double dt_used = dt;
-      (void)dt_used;
 
       // Stages (rk.rs:370-384): scratch = y + sum_j M[i][j] K_j; K_i = f(.) * dt.
       static_for<0, S>([&](auto ic) {
@@ -267,6 +266,21 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
         ++acc;
       } else {
         ++rej;
+        // A rejection that leaves dt bitwise unchanged (the factor rounded to
+        // exactly 1) with finite stages makes the next attempt identical: the
+        // tableau reads only this attempt's stages (every layout but
+        // as_compiled), so every attempt up to the cap is rejected the same
+        // way and the reference would loop forever.  Jump to the cap with the
+        // counts those attempts would leave.
+        if constexpr (Tab::kLayout != kAsCompiled) {
+          uint32_t bad = 0u;
+#pragma unroll
+          for (int j = 0; j < S; ++j) bad |= kbad[j];
+          if (bad == 0u && dt == dt_used) {
+            rej += static_cast<int32_t>(a.max_attempts - attempts);
+            attempts = a.max_attempts;
+          }
+        }
       }
     }
 

@@ -340,3 +340,88 @@ def bdf_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=BDF6, m
         raise IVPError(code, _capi.last_error())
     return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code),
                     out.get("traj_t"), out.get("traj_y"))
+
+
+@dataclass
+class RaggedSolution:
+    """Per-system outcome of a ragged solve: y is flat, system i's final state
+    is y[y_off[i]:y_off[i+1]]."""
+    y: Any
+    t: Any
+    accepted: Any
+    rejected: Any
+    status: Any
+    code: int
+
+
+def _alloc_ragged(total: int, n: int, device: bool):
+    if device:
+        import torch
+        dev = torch.device("cuda")
+        return dict(y=torch.empty(total, dtype=torch.float64, device=dev),
+                    t=torch.empty(n, dtype=torch.float64, device=dev),
+                    accepted=torch.empty(n, dtype=torch.int32, device=dev),
+                    rejected=torch.empty(n, dtype=torch.int32, device=dev),
+                    status=torch.empty(n, dtype=torch.int32, device=dev))
+    return dict(y=np.empty(total), t=np.empty(n), accepted=np.empty(n, np.int32),
+                rejected=np.empty(n, np.int32), status=np.empty(n, np.int32))
+
+
+def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_steps=0,
+                    ctx: Context | None = None, blocks_per_sm=0, uniform_out=None, ragged_out=None,
+                    raise_on_error=False):
+    """One launch of the corrected BDF over a stiff batch of a uniform part
+    (attributes y0 (dim, n), params, t0, t_end, rhs, tol, dt_min, dt_max, as
+    workloads.Batch) and a ragged part (y_off, p_off, flat y0 and params, t0,
+    t_end, rhs, tol, dt_min, dt_max, as workloads.RaggedBatch).  Arrays are
+    all numpy (host) or all CUDA tensors.  Returns (Solution | None,
+    RaggedSolution | None)."""
+    ctx = ctx or default_context()
+    first = uniform.y0 if uniform is not None else ragged.y0
+    device = _is_device(first)
+    prob = None
+    uout = None
+    if uniform is not None:
+        prob = make_problem(uniform.y0, uniform.params, uniform.t0, uniform.t_end, uniform.tol,
+                            uniform.dt_min, uniform.dt_max, uniform.rhs)
+        dim, n = int(uniform.y0.shape[0]), int(uniform.y0.shape[1])
+        uout = uniform_out if uniform_out is not None else alloc_outputs(dim, n, device)
+    rp = None
+    rout = None
+    if ragged is not None:
+        rp = _capi.RaggedProblem()
+        rp.n = int(ragged.y_off.shape[0]) - 1
+        rp.rhs = int(ragged.rhs)
+        rp.y_offsets, rp.p_offsets = _ptr(ragged.y_off), _ptr(ragged.p_off)
+        rp.y0, rp.params = _ptr(ragged.y0), _ptr(ragged.params)
+        for name in ("t0", "t_end"):
+            v = getattr(ragged, name)
+            if np.isscalar(v):
+                setattr(rp, name, None)
+                setattr(rp, name + "_scalar", float(v))
+            else:
+                setattr(rp, name, _ptr(v))
+        rp.tol, rp.dt_min, rp.dt_max = float(ragged.tol), float(ragged.dt_min), float(ragged.dt_max)
+        rout = ragged_out if ragged_out is not None else _alloc_ragged(int(ragged.y0.shape[0]), rp.n, device)
+    o = _capi.BdfOptions()
+    o.method, o.mode, o.memory = method, BDF_CORRECTED, MEM_DEVICE if device else MEM_HOST
+    o.max_iter, o.max_steps, o.block, o.blocks_per_sm = int(max_iter), int(max_steps), 0, int(blocks_per_sm)
+    ures = make_result(uout, 0) if uout is not None else None
+    rres = None
+    if rout is not None:
+        rres = _capi.RaggedResult()
+        rres.y_final, rres.t_final = _ptr(rout["y"]), _ptr(rout["t"])
+        rres.accepted, rres.rejected, rres.status = _ptr(rout["accepted"]), _ptr(rout["rejected"]), _ptr(rout["status"])
+    code = _capi.load().bacon_bdf_solve_mixed(ctx.handle, ctypes.byref(prob) if prob is not None else None,
+                                              ctypes.byref(rp) if rp is not None else None, ctypes.byref(o),
+                                              ctypes.byref(ures) if ures is not None else None,
+                                              ctypes.byref(rres) if rres is not None else None)
+    if code in (14, 15, 16) or (raise_on_error and code != 0):
+        raise IVPError(code, _capi.last_error())
+    us = None
+    if uout is not None:
+        us = Solution(uout["y"], uout["t"], uout["accepted"], uout["rejected"], uout["status"], int(code))
+    rs = None
+    if rout is not None:
+        rs = RaggedSolution(rout["y"], rout["t"], rout["accepted"], rout["rejected"], rout["status"], int(code))
+    return us, rs

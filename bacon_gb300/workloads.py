@@ -128,3 +128,75 @@ def linear_shared(n: int = 1 << 16, dim: int = 256, seed: int = 4) -> Batch:
     return Batch("linear_shared", RHS_LINEAR, y0, np.zeros((0, n)), np.zeros(n), np.full(n, 5.0),
                  1e-8, 1e-10, 0.1, seed, {"A": np.ascontiguousarray(A), "Q": q, "lambda": lam,
                                           "exact": exact})
+
+
+@dataclass
+class RaggedBatch:
+    """Systems of one right-hand side with uneven sizes, packed flat: system
+    i's state is y0[y_off[i]:y_off[i+1]], its parameters
+    params[p_off[i]:p_off[i+1]]."""
+    name: str
+    rhs: int
+    y_off: np.ndarray       # (n+1,) int64
+    p_off: np.ndarray       # (n+1,) int64
+    y0: np.ndarray          # (y_off[n],)
+    params: np.ndarray      # (p_off[n],)
+    t0: np.ndarray          # (n,)
+    t_end: np.ndarray       # (n,)
+    tol: float
+    dt_min: float
+    dt_max: float
+    seed: int
+
+    @property
+    def n(self) -> int:
+        return self.y_off.shape[0] - 1
+
+    @property
+    def dims(self) -> np.ndarray:
+        return np.diff(self.y_off)
+
+    def system(self, i: int):
+        """(y0_i, params_i) of system i."""
+        return (self.y0[self.y_off[i]:self.y_off[i + 1]], self.params[self.p_off[i]:self.p_off[i + 1]])
+
+    def subset(self, idx) -> "RaggedBatch":
+        idx = np.asarray(idx)
+        ys = [self.y0[self.y_off[i]:self.y_off[i + 1]] for i in idx]
+        ps = [self.params[self.p_off[i]:self.p_off[i + 1]] for i in idx]
+        y_off = np.concatenate([[0], np.cumsum([len(y) for y in ys])]).astype(np.int64)
+        p_off = np.concatenate([[0], np.cumsum([len(p) for p in ps])]).astype(np.int64)
+        return RaggedBatch(self.name, self.rhs, y_off, p_off,
+                           np.concatenate(ys) if ys else np.zeros(0),
+                           np.concatenate(ps) if ps else np.zeros(0), self.t0[idx].copy(),
+                           self.t_end[idx].copy(), self.tol, self.dt_min, self.dt_max, self.seed)
+
+
+def ragged_spring_chains(n: int = 1 << 16, min_masses: int = 2, max_masses: int = 64,
+                         seed: int = 7) -> RaggedBatch:
+    """Damped spring-mass chains of uneven length: m_i ~ U{min..max} unit
+    masses (dim 2 m_i), with spring_chains' value distributions per system:
+    k = 10^U[0, 6] (stiffness ratio up to 1e6), c = 2 sqrt(max k), x0 ~
+    U[-1, 1], v0 = 0, t in [0, 10], tol 1e-6, dt in [1e-12, 1]."""
+    rng = np.random.default_rng(seed)
+    m = rng.integers(min_masses, max_masses + 1, n)
+    y_off = np.concatenate([[0], np.cumsum(2 * m)]).astype(np.int64)
+    p_off = np.concatenate([[0], np.cumsum(m + 1)]).astype(np.int64)
+    y0 = np.zeros(int(y_off[-1]))
+    params = np.empty(int(p_off[-1]))
+    for i in range(n):
+        mi = int(m[i])
+        k = 10.0 ** rng.uniform(0.0, 6.0, mi)
+        params[p_off[i]:p_off[i] + mi] = k
+        params[p_off[i] + mi] = 2.0 * np.sqrt(k.max())
+        y0[y_off[i]:y_off[i] + mi] = rng.uniform(-1.0, 1.0, mi)
+    return RaggedBatch("ragged_spring_chains", RHS_CHAIN, y_off, p_off, y0, params, np.zeros(n),
+                       np.full(n, 10.0), 1e-6, 1e-12, 1.0, seed)
+
+
+def stiff_batch(n: int = 131072, seed: int = 8):
+    """The stiff BDF6 batch: n/2 Robertson systems (robertson()) and n/2
+    spring-mass chains with m ~ U{2..64} masses (ragged_spring_chains()).
+    Returns (Batch, RaggedBatch)."""
+    half = n // 2
+    return robertson(n=half, seed=seed), ragged_spring_chains(n=n - half, seed=seed + 1)

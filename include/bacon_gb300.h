@@ -233,6 +233,53 @@ typedef struct {
 int bacon_bdf_solve(bacon_ctx* ctx, const bacon_problem* problem,
                     const bacon_bdf_options* options, bacon_rk_result* result);
 
+/* A batch of systems of one right-hand side whose sizes differ.  System i's
+ * state is y0[y_offsets[i] .. y_offsets[i+1]) and its parameters
+ * params[p_offsets[i] .. p_offsets[i+1]).  In the reference each is its own
+ * solver over a DVector state (bdf.rs:257-333 builds one per system), so norms
+ * take nalgebra's dynamic-vector order.  Right-hand sides: BACON_RHS_CHAIN
+ * (dim 2 m_i for m_i = 1..64 masses, m_i + 1 parameters: k_1..k_{m_i}, c). */
+typedef struct {
+  int64_t n;
+  int32_t rhs;
+  int32_t reserved;
+  const int64_t* y_offsets; /* [n+1], y_offsets[0] = 0 */
+  const int64_t* p_offsets; /* [n+1], p_offsets[0] = 0 */
+  const double* y0;         /* [y_offsets[n]] */
+  const double* params;     /* [p_offsets[n]] */
+  const double* t0;         /* [n] or NULL: t0_scalar */
+  const double* t_end;      /* [n] or NULL: t_end_scalar */
+  double t0_scalar, t_end_scalar;
+  double tol, dt_min, dt_max;
+} bacon_ragged_problem;
+
+typedef struct {
+  double* y_final;   /* [y_offsets[n]] last yielded state */
+  double* t_final;   /* [n] */
+  int32_t* accepted; /* [n] */
+  int32_t* rejected; /* [n] */
+  int32_t* status;   /* [n] */
+} bacon_ragged_result;
+
+/* Checks a ragged batch whose offsets are host arrays: rhs CHAIN, offsets
+ * from 0, every dim even in 2..128 with dim/2 + 1 parameters, tol > 0, dt
+ * bounds > 0.  BACON_OK or BACON_INVALID_ARGUMENT / BACON_UNSUPPORTED. */
+int bacon_ragged_validate(const bacon_ragged_problem* problem);
+
+/* One launch of the corrected BDF (BDF6 / BDF2) over a stiff batch of two
+ * parts: a uniform batch of small systems (one thread each, as
+ * bacon_bdf_solve; uniform rhs ROBERTSON or VDP) and a ragged batch (one warp
+ * each, largest first; LU factors in a per-warp device workspace).  Either
+ * part may be NULL, not both.  Same memory kind for every array
+ * (options->memory).  Results are bit-identical to solving each system alone
+ * with the corrected BDF.  Returns BACON_OK or the status of the lowest
+ * failing ragged system, else of the lowest failing uniform system. */
+int bacon_bdf_solve_mixed(bacon_ctx* ctx, const bacon_problem* uniform,
+                          const bacon_ragged_problem* ragged,
+                          const bacon_bdf_options* options,
+                          bacon_rk_result* uniform_result,
+                          bacon_ragged_result* ragged_result);
+
 /* ---- discrete adjoint ---------------------------------------------------- */
 /* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with
  * respect to its initial state and parameters, through the accepted-step

@@ -1,0 +1,123 @@
+"""Ragged (uneven-size) stiff batches: one warp per spring-mass chain, and the
+mixed Robertson + chains launch, bit for bit against the CPU oracle's
+corrected BDF (each chain a dynamically sized system) and against the
+one-thread-per-system kernel for the uniform part."""
+import numpy as np
+import pytest
+
+from bacon_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+# sizes around the 32-row chunk boundaries of the warp layout (dim = 2 m)
+MASSES = [1, 2, 3, 5, 8, 15, 16, 17, 24, 31, 32, 33, 40, 47, 48, 49, 63, 64]
+
+
+def _chains(masses, seed, t_end):
+    rng = np.random.default_rng(seed)
+    base = W.ragged_spring_chains(n=len(masses), min_masses=1, max_masses=1, seed=seed)
+    ys, ps = [], []
+    for m in masses:
+        k = 10.0 ** rng.uniform(0.0, 6.0, m)
+        ps.append(np.concatenate([k, [2.0 * np.sqrt(k.max())]]))
+        y = np.zeros(2 * m)
+        y[:m] = rng.uniform(-1.0, 1.0, m)
+        ys.append(y)
+    base.y_off = np.concatenate([[0], np.cumsum([len(y) for y in ys])]).astype(np.int64)
+    base.p_off = np.concatenate([[0], np.cumsum([len(p) for p in ps])]).astype(np.int64)
+    base.y0 = np.concatenate(ys)
+    base.params = np.concatenate(ps)
+    base.t_end = np.full(len(masses), t_end)
+    base.t0 = np.zeros(len(masses))
+    return base
+
+
+def _oracle_ragged(O, r, method=0, max_steps=200000):
+    cfg = O.bdf_cfg(method=method, mode=O.BDF_CORRECTED, dyn_dim=True, tol=r.tol, dt_min=r.dt_min,
+                    dt_max=r.dt_max, max_steps=max_steps)
+    out = {"y": np.zeros_like(r.y0), "t": np.zeros(r.n), "accepted": np.zeros(r.n, np.int64),
+           "rejected": np.zeros(r.n, np.int64), "status": np.zeros(r.n, np.int32)}
+    for i in range(r.n):
+        y0, p = r.system(i)
+        res = O.bdf_solve_one(cfg, r.rhs, y0, r.t0[i], r.t_end[i], params=p)
+        out["y"][r.y_off[i]:r.y_off[i + 1]] = res.y
+        out["t"][i] = res.t
+        out["accepted"][i] = res.accepted
+        out["rejected"][i] = res.rejected
+        out["status"][i] = res.status
+    return out
+
+
+def _same(sol, ref):
+    np.testing.assert_array_equal(sol.status, ref["status"])
+    np.testing.assert_array_equal(sol.accepted, ref["accepted"])
+    np.testing.assert_array_equal(sol.rejected, ref["rejected"])
+    np.testing.assert_array_equal(sol.t, ref["t"])
+    np.testing.assert_array_equal(sol.y.view(np.int64), ref["y"].view(np.int64))
+
+
+def test_ragged_chains_bit_exact(engine, oracle):
+    r = _chains(MASSES, seed=31, t_end=0.3)
+    _, sol = engine.bdf_solve_mixed(None, r)
+    ref = _oracle_ragged(oracle, r)
+    assert (ref["status"] == 0).all()
+    _same(sol, ref)
+
+
+def test_ragged_chains_bdf2_bit_exact(engine, oracle):
+    """BDF2's order-1/order-2 error estimate keeps dt near 1e-7 on these
+    chains, so the horizon is short."""
+    r = _chains([1, 3, 16, 17], seed=32, t_end=1e-3)
+    _, sol = engine.bdf_solve_mixed(None, r, method=1)
+    ref = _oracle_ragged(oracle, r, method=1)
+    assert (ref["status"] == 0).all()
+    _same(sol, ref)
+
+
+def test_ragged_chains_full_horizon_sample(engine, oracle):
+    """The workload's own distribution (m ~ U{2..64}) over t in [0, 10]."""
+    r = W.ragged_spring_chains(n=12, seed=7)
+    _, sol = engine.bdf_solve_mixed(None, r)
+    ref = _oracle_ragged(oracle, r)
+    _same(sol, ref)
+
+
+def test_mixed_launch_matches_parts(engine, oracle):
+    """Robertson (a thread each) and chains (a warp each) in one launch: the
+    uniform part equals bacon_bdf_solve, the ragged part the oracle."""
+    rob = W.robertson(n=300, seed=41)
+    r = _chains(MASSES[::2], seed=42, t_end=0.2)
+    us, rs = engine.bdf_solve_mixed(rob, r)
+    alone = engine.bdf_solve(rob.y0, rob.params, rob.t0, rob.t_end, rhs=rob.rhs, tol=rob.tol,
+                             dt_min=rob.dt_min, dt_max=rob.dt_max, mode=engine.BDF_CORRECTED)
+    np.testing.assert_array_equal(us.status, alone.status)
+    np.testing.assert_array_equal(us.accepted, alone.accepted)
+    np.testing.assert_array_equal(us.rejected, alone.rejected)
+    np.testing.assert_array_equal(us.y.view(np.int64), alone.y.view(np.int64))
+    _same(rs, _oracle_ragged(oracle, r))
+
+
+def test_mixed_device_arrays(engine, oracle):
+    torch = pytest.importorskip("torch")
+    r = _chains([4, 33, 64], seed=43, t_end=0.2)
+    dev = torch.device("cuda")
+    d = W.RaggedBatch(r.name, r.rhs, *(torch.from_numpy(x).to(dev) for x in (r.y_off, r.p_off, r.y0, r.params,
+                                                                               r.t0, r.t_end)),
+                      r.tol, r.dt_min, r.dt_max, r.seed)
+    _, sol = engine.bdf_solve_mixed(None, d)
+    ref = _oracle_ragged(oracle, r)
+    np.testing.assert_array_equal(sol.y.cpu().numpy().view(np.int64), ref["y"].view(np.int64))
+    np.testing.assert_array_equal(sol.accepted.cpu().numpy(), ref["accepted"])
+
+
+def test_ragged_failures_retire_only_their_system(engine, oracle):
+    r = _chains([3, 20, 40], seed=44, t_end=0.2)
+    r.t_end = r.t_end.copy()
+    r.t_end[1] = -1.0   # ends before it starts
+    r.y0 = r.y0.copy()
+    r.y0[r.y_off[2]] = np.nan
+    _, sol = engine.bdf_solve_mixed(None, r, max_steps=500)
+    ref = _oracle_ragged(oracle, r, max_steps=500)
+    assert sol.status[0] == 0 and sol.status[1] == 5 and sol.status[2] != 0
+    np.testing.assert_array_equal(sol.status, ref["status"])
+    assert sol.code == 5

@@ -154,3 +154,40 @@ def test_python_builder_errors(capi):
     assert e.value.variant == "MissingParameters"
     b = RungeKutta45.new(2).with_start(0.0).with_end(1.0).build()
     assert b.dim() == 2
+
+
+def test_ragged_validation_without_gpu():
+    """Ragged batches are checked on the host before any device work."""
+    import ctypes
+
+    from bacon_gb300 import _capi
+    from bacon_gb300 import workloads as W
+
+    lib = _capi.load()
+    r = W.ragged_spring_chains(n=3, seed=1)
+    keep = []
+
+    def check(y_off=None, p_off=None, rhs=W.RHS_CHAIN, tol=1e-6, dt_min=1e-12):
+        y_off = np.ascontiguousarray(r.y_off if y_off is None else y_off, dtype=np.int64)
+        p_off = np.ascontiguousarray(r.p_off if p_off is None else p_off, dtype=np.int64)
+        keep.extend([y_off, p_off])
+        rp = _capi.RaggedProblem()
+        rp.n = len(y_off) - 1
+        rp.rhs = rhs
+        rp.y_offsets, rp.p_offsets = y_off.ctypes.data, p_off.ctypes.data
+        rp.y0, rp.params = r.y0.ctypes.data, r.params.ctypes.data
+        rp.tol, rp.dt_min, rp.dt_max = tol, dt_min, 1.0
+        return lib.bacon_ragged_validate(ctypes.byref(rp))
+
+    assert check() == 0
+    assert check(rhs=W.RHS_VDP) == 16
+    assert check(tol=0.0) == 15
+    assert check(dt_min=0.0) == 15
+    assert check(y_off=[0, 3], p_off=[0, 2]) == 15          # odd dim
+    assert check(y_off=[0, 130], p_off=[0, 66]) == 15       # dim above 128
+    assert check(y_off=[0, 0], p_off=[0, 1]) == 15          # dim 0
+    assert check(y_off=[0, 4], p_off=[0, 2]) == 15          # chain of 2 masses takes 3 params
+    assert check(y_off=[1, 5], p_off=[0, 3]) == 15          # offsets must start at 0
+    assert check(y_off=[0, 128], p_off=[0, 65]) == 0        # 64 masses
+    o = _capi.BdfOptions()
+    assert lib.bacon_bdf_solve_mixed(None, None, None, ctypes.byref(o), None, None) == 15

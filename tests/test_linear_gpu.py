@@ -41,13 +41,20 @@ def test_linear_fma_close_to_exact_solution(engine):
 @pytest.mark.parametrize("dim", [128, 256])
 def test_linear_tensor_core_split(engine, dim):
     """tcgen05 stage GEMM with 6 x 6-bit bf16 slices: the product A*Y is exact
-    to ~2^-36 relative, so the engine takes the FP64 engine's steps and
-    reaches the same accuracy against the exact solution."""
+    to ~2^-36 relative, so the engine reaches the FP64 engine's accuracy
+    against the exact solution and nearly its step counts.  With the
+    reference's safety factor 1 a rejection lands the next attempt at
+    err ~ tol, so any perturbation (the FMA engine's too) flips some accept
+    decisions: the step counts agree about as often as FMA's do with exact."""
     b = W.linear_shared(n=1024, dim=dim, seed=23)
     ex = b.extra["exact"](5.0)
     fp = _solve(engine, b, precision=0)
+    fma = _solve(engine, b, precision=1)
     tc = _solve(engine, b, precision=engine.TC_SPLIT)
     assert (tc.status == 0).all()
     assert np.abs(tc.y - ex).max() < 1e-7
-    assert np.mean(tc.accepted == fp.accepted) >= 0.99
+    same_tc = np.mean(tc.accepted == fp.accepted)
+    same_fma = np.mean(fma.accepted == fp.accepted)
+    assert same_tc >= 0.95 and same_tc >= same_fma - 0.03, (same_tc, same_fma)
+    assert np.abs(tc.accepted.astype(np.int64) - fp.accepted).max() <= 3
     assert np.abs(tc.y - fp.y).max() < 1e-8

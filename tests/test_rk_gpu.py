@@ -185,3 +185,23 @@ def test_reference_unit_tests_quadratic_and_sine(engine, kind):
         assert len(path) > 0
         for t, y in path:
             assert abs(y[0] - np.sin(t)) <= 0.01
+
+
+def test_stuck_controller_jumps_to_the_cap(engine, oracle):
+    """Two Lotka-Volterra systems of the adjoint workload reach a rejection
+    whose step factor rounds to exactly 1, so dt never changes and the
+    reference would retry forever.  The engine jumps straight to the attempt
+    cap with the same counts the attempt-by-attempt loop (the oracle) ends
+    with, and without the jump a 10,000,000-attempt cap would take minutes."""
+    import time
+    full = W.lotka_volterra(n=1 << 18)
+    b = full.subset(np.array([1574, 181858, 0, 1, 2]))
+    ref = _oracle_batch(oracle, b, max_attempts=100000)
+    assert list(ref["status"][:2]) == [13, 13] and (ref["status"][2:] == 0).all()
+    _assert_identical(_gpu_batch(engine, b, max_attempts=100000), ref)
+    t0 = time.perf_counter()
+    sol = _gpu_batch(engine, b)  # default cap 10,000,000
+    assert time.perf_counter() - t0 < 5.0
+    assert list(sol.status[:2]) == [13, 13]
+    np.testing.assert_array_equal(sol.accepted[:2] + sol.rejected[:2], [10_000_000, 10_000_000])
+    np.testing.assert_array_equal(sol.accepted, ref["accepted"])
