@@ -17,21 +17,23 @@
 
 namespace bacon {
 
-// log2(num / den) for num > 0 and den >= 0 over the whole double range, to
-// float accuracy near 1: the exponent difference as an integer plus log2 of
-// the ratio of the two mantissas (both in [1, 2), so the float quotient lies
-// in (1/2, 2) and neither over- nor underflows however small (tol*dt)^2 gets).
-// A zero den gives +inf, a NaN den NaN, an infinite den -inf.
+// log2(num / den) for non-negative num and den over the whole double range,
+// from the bit patterns with integer operations only (no FP64 instruction):
+// the exponent difference plus log2f of the quotient of the two mantissas,
+// each truncated to a float in [1, 2), so the quotient lies in (1/2, 2) and
+// nothing under- or overflows however small (tol*dt)^2 gets.  Accurate to
+// ~2^-22, ample for a step factor.  den = 0 gives +inf, a NaN den NaN, an
+// infinite den or num = 0 -inf (subnormal operands read as 2^-1023 * m).
 __device__ __forceinline__ float log2_ratio(double num, double den) {
-  if (!(den > 0.0)) return (den == 0.0) ? INFINITY : __int_as_float(0x7fc00000);
-  if (__double2hiint(den) >= 0x7ff00000) return -INFINITY;
-  if (!(num > 0.0)) return -INFINITY;
-  const int hn = __double2hiint(num), hd = __double2hiint(den);
-  const int e = ((hn >> 20) & 0x7ff) - ((hd >> 20) & 0x7ff);
-  const double mn = __hiloint2double((hn & 0x000fffff) | 0x3ff00000, __double2loint(num));
-  const double md = __hiloint2double((hd & 0x000fffff) | 0x3ff00000, __double2loint(den));
-  const float q = __fdiv_rn(__double2float_rn(mn), __double2float_rn(md));
-  return static_cast<float>(e) + log2f(q);
+  const long long bn = __double_as_longlong(num), bd = __double_as_longlong(den);
+  constexpr long long kInf = 0x7ff0000000000000ll;
+  if (bd > kInf) return __int_as_float(0x7fc00000);
+  if (bd == 0) return INFINITY;
+  if (bd == kInf || bn == 0) return -INFINITY;
+  const int e = static_cast<int>(bn >> 52) - static_cast<int>(bd >> 52);
+  const float mn = __int_as_float(0x3f800000 | static_cast<int>((bn >> 29) & 0x7fffff));
+  const float md = __int_as_float(0x3f800000 | static_cast<int>((bd >> 29) & 0x7fffff));
+  return static_cast<float>(e) + log2f(__fdiv_rn(mn, md));
 }
 
 // Largest factor a rejected attempt may keep: 1 - 2^-20.  The reference's

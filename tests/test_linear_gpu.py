@@ -57,4 +57,5 @@ def test_linear_tensor_core_split(engine, dim):
     same_fma = np.mean(fma.accepted == fp.accepted)
     assert same_tc >= 0.95 and same_tc >= same_fma - 0.03, (same_tc, same_fma)
     assert np.abs(tc.accepted.astype(np.int64) - fp.accepted).max() <= 3
-    assert np.abs(tc.y - fp.y).max() < 1e-8
+    # different accept decisions on a few systems move their states by ~tol
+    assert np.abs(tc.y - fp.y).max() < 5e-8
