@@ -255,10 +255,16 @@ namespace {
 // two 128-thread CTAs per SM, while every extra resident thread lengthens the
 // tail in which lanes run out of systems.  Aim for >= 16 systems per thread
 // and at least 256 threads per SM.
-int model_blocks_per_sm(int64_t n, int num_sms, int block, int max_bps) {
+// Persistent CTAs per SM: enough threads that every thread still has ~16
+// systems (so the longest-first order balances the tail), at least
+// min_threads per SM, at most 4 CTAs.  The FP64-bound kernels run at the same
+// speed from 256 to 512 threads per SM; the FP32-stage kernel is latency bound
+// and asks for 768 (measured on Lorenz 1M: 211 ms at 256 threads, 157 ms at
+// 768 or more).
+int model_blocks_per_sm(int64_t n, int num_sms, int block, int max_bps, int min_threads = 256) {
   const int64_t threads_for_tail = n / 16;
   int64_t bps = threads_for_tail / (static_cast<int64_t>(num_sms) * block);
-  const int64_t floor_bps = (256 + block - 1) / block;
+  const int64_t floor_bps = (min_threads + block - 1) / block;
   if (bps < floor_bps) bps = floor_bps;
   if (bps > 4) bps = 4;
   if (bps > max_bps) bps = max_bps;
@@ -637,12 +643,13 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
       bps = it->second.second;
     }
   }
-  if (block == 0) block = 128;
+  const bool ff = opt->precision == BACON_FP32_COMP;
+  if (block == 0) block = ff ? 256 : 128;
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
   if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
-  if (bps == 0) bps = model_blocks_per_sm(p->n, c->num_sms, block, max_bps);
+  if (bps == 0) bps = model_blocks_per_sm(p->n, c->num_sms, block, max_bps, ff ? 768 : 256);
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(c->num_sms) * bps;
   const long long need = (p->n + block - 1) / block;
