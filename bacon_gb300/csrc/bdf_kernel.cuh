@@ -134,6 +134,7 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
 #pragma unroll
     for (int k = 0; k < D; ++k) M[r][k] = O::sub((r == k) ? 1.0 : 0.0, O::mul(hb, M[r][k]));
   int piv[D];
+  double rinv[D];  // 1 / U[i][i], the elimination's own reciprocal
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     int pr = i;
@@ -161,6 +162,7 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
     }
     if (M[i][i] == 0.0) return false;
     const double inv = O::div(1.0, M[i][i]);
+    rinv[i] = inv;
 #pragma unroll
     for (int r = i + 1; r < D; ++r) {
       const double l = O::mul(M[r][i], inv);
@@ -194,7 +196,7 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
       for (int r = i + 1; r < D; ++r) dx[r] = O::sub(dx[r], O::mul(M[r][i], dx[i]));
 #pragma unroll
     for (int i = D - 1; i >= 0; --i) {
-      dx[i] = O::div(dx[i], M[i][i]);
+      dx[i] = O::mul(dx[i], rinv[i]);
 #pragma unroll
       for (int r = 0; r < i; ++r) dx[r] = O::sub(dx[r], O::mul(M[r][i], dx[i]));
     }

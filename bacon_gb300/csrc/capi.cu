@@ -110,7 +110,8 @@ struct bacon_ctx {
   cudaStream_t stream = nullptr;
   int num_sms = 0;
   // [0] work counter [1] first failing index [2] live [3] adjoint queue /
-  // tensor-core error flag [4] ragged work counter [5] first failing ragged index
+  // tensor-core error flag [5] first failing ragged index [8..11] ragged work
+  // counters, one per size class
   unsigned long long* d_ctl = nullptr;
   unsigned long long* h_ctl = nullptr;  // pinned mirror
   std::vector<bacon::RkEntry> kernels;
@@ -132,8 +133,7 @@ struct bacon_ctx {
   DevBuf adj_dt, adj_ck, adj_tgt, adj_loss, adj_gy, adj_gp;
   DevBuf lin_A, lin_y, lin_K, lin_t, lin_dt, lin_end, lin_att;
   DevBuf tc_sa, tc_ea, tc_sy, tc_ey;
-  DevBuf rg_yoff, rg_poff, rg_y0, rg_p, rg_t0, rg_te, rg_yout, rg_tout, rg_acc, rg_rej, rg_st, rg_ord, rg_lu,
-      rg_perm;
+  DevBuf rg_yoff, rg_poff, rg_y0, rg_p, rg_t0, rg_te, rg_yout, rg_tout, rg_acc, rg_rej, rg_st, rg_ord, rg_lu;
 };
 
 extern "C" {
@@ -151,8 +151,8 @@ int bacon_ctx_create(int device, bacon_ctx** out) {
   c->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&c->d_ctl), 8 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->h_ctl), 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&c->d_ctl), 16 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->h_ctl), 16 * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     delete c;
     return fail(BACON_CUDA_ERROR, std::string("bacon_ctx_create: ") + cudaGetErrorString(e));
@@ -508,7 +508,9 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   }
   __nv_bfloat16* sy = c->tc_sy.as<__nv_bfloat16>();
   int32_t* ey = c->tc_ey.as<int32_t>();
-  const dim3 tg(static_cast<unsigned>((n + bacon::kTcN - 1) / bacon::kTcN), static_cast<unsigned>(D / bacon::kTcM));
+  // persistent stage GEMM: one CTA per SM over (systems / 64) x (D / 128) tiles
+  const long long tc_tiles = ((n + bacon::kTcN - 1) / bacon::kTcN) * (D / bacon::kTcM);
+  const dim3 tg(static_cast<unsigned>(tc_tiles < c->num_sms ? tc_tiles : c->num_sms));
   BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
   while (*h_live > 0) {
     for (int s = 0; s < k.stages; ++s) {
@@ -967,15 +969,26 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   }
   if (un == 0 && gn == 0) return BACON_OK;
   BACON_CUDA(cudaSetDevice(c->device));
+  // work order: size classes in kernel phase order, largest dim first within
+  // a class (longest-first scheduling)
   std::vector<uint32_t> order(gn);
   for (int64_t i = 0; i < gn; ++i) order[i] = static_cast<uint32_t>(i);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](uint32_t a, uint32_t b) { return yo[a + 1] - yo[a] > yo[b + 1] - yo[b]; });
+  auto dim_of = [&](uint32_t i) { return static_cast<int>(yo[i + 1] - yo[i]); };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+    const int ca = bacon::rag_class_of(dim_of(a)), cb = bacon::rag_class_of(dim_of(b));
+    return ca != cb ? ca < cb : dim_of(a) > dim_of(b);
+  });
+  int64_t class_n[bacon::kRagClasses] = {0, 0, 0, 0};
+  unsigned class_mask = 0;
+  for (int64_t i = 0; i < gn; ++i) {
+    const int cl = bacon::rag_class_of(dim_of(static_cast<uint32_t>(i)));
+    ++class_n[cl];
+    class_mask |= 1u << cl;
+  }
 
-  // launch shape
-  const int block = 128;
-  const int warps = block / 32;
-  const size_t smem = gn > 0 ? static_cast<size_t>(warps) * bacon::rag_smem_doubles(ld) * sizeof(double) : 0;
+  // launch shape: one CTA of 8 warps per SM (its shared memory fills the SM)
+  const int block = bacon::kRagWarps * 32;
+  const size_t smem = bacon::rag_cta_smem_bytes(class_mask);
   BACON_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, smem));
@@ -1022,9 +1035,12 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   rg.max_steps = a.max_steps;
   rg.max_iter = a.max_iter;
   rg.qmax = a.qmax;
-  rg.queue = c->d_ctl + 4;
+  rg.queues = c->d_ctl + 8;
   rg.first_fail = c->d_ctl + 5;
-  rg.ld = ld;
+  for (int cl = 0, start = 0; cl < bacon::kRagClasses; start += static_cast<int>(class_n[cl]), ++cl) {
+    rg.class_start[cl] = start;
+    rg.class_n[cl] = class_n[cl];
+  }
   const size_t ytot = gn > 0 ? static_cast<size_t>(yo[gn]) : 0;
   const size_t ptot = gn > 0 ? static_cast<size_t>(po[gn]) : 0;
   if (gn > 0) {
@@ -1036,11 +1052,8 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
     const size_t nn = static_cast<size_t>(gn);
     BACON_CUDA(c->rg_ord.ensure(nn * sizeof(uint32_t)));
     rg.order = c->rg_ord.as<uint32_t>();
-    const size_t slots = static_cast<size_t>(grid) * warps;
-    BACON_CUDA(c->rg_lu.ensure(slots * 2 * ld * ld * sizeof(double)));
-    BACON_CUDA(c->rg_perm.ensure(slots * 2 * ld * sizeof(int32_t)));
-    rg.lu = c->rg_lu.as<double>();
-    rg.perm = c->rg_perm.as<int32_t>();
+    BACON_CUDA(c->rg_lu.ensure(static_cast<size_t>(grid) * bacon::rag_gcache_cta_doubles() * sizeof(double)));
+    rg.gcache = c->rg_lu.as<double>();
     if (host) {
       BACON_CUDA(c->rg_yoff.ensure((nn + 1) * sizeof(int64_t)));
       BACON_CUDA(c->rg_poff.ensure((nn + 1) * sizeof(int64_t)));
@@ -1110,7 +1123,7 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   }
   BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
   BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
-  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 4, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 8, 0, bacon::kRagClasses * sizeof(unsigned long long), c->stream));
   BACON_CUDA(cudaMemsetAsync(c->d_ctl + 5, 0xff, sizeof(unsigned long long), c->stream));
   void* args[] = {&a, &dyn, &rg};
   BACON_CUDA(cudaEventRecord(c->ev0, c->stream));

@@ -20,7 +20,7 @@ void fill_tc(LinTcKernels& k) {
     k.slice[5] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 5>);
   }
   k.gemm = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D>);
-  k.smem_bytes = kTcSlices * (kTcM * kTcKc * 2 + kTcN * kTcKc * 2);
+  k.smem_bytes = 2 * kTcBufBytes;
   k.slices = kTcSlices;
 }
 

@@ -31,7 +31,7 @@ constexpr int kTcSlices = 6;      // slices per operand (36 bits)
 constexpr int kTcBits = 6;        // bits per slice
 constexpr int kTcM = 128;         // rows per CTA
 constexpr int kTcN = 64;          // systems per CTA
-constexpr int kTcKc = 64;         // K per shared-memory chunk
+constexpr int kTcKc = 32;         // K per shared-memory chunk (two buffers)
 constexpr int kTcTmemCols = 512;  // kTcSlices accumulators x 64 columns, rounded to a power of two
 
 struct TcArgs {
@@ -116,30 +116,68 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // --- the stage GEMM ------------------------------------------------------------
-// Shared memory: A slices for one chunk [NS][128 x 64] (16 KiB each), B slices
-// [NS][64 x 64] (8 KiB each): 144 KiB, plus the mbarrier and TMEM address.
+// Persistent: one CTA per SM walks the (64-system, 128-row) tiles.  K = D is
+// staged in chunks of 32 with cp.async into two buffers, each holding the A
+// slices [NS][128 x 32] (8 KiB each) and B slices [NS][64 x 32] (4 KiB each):
+// 2 x 72 KiB.  The chunk after the current one loads while the tensor cores
+// work on the current one; the buffer it overwrites is released by the
+// mbarrier its last MMAs committed to.  Every wait is bounded.
+constexpr int kTcBufBytes = kTcSlices * (kTcM + kTcN) * kTcKc * 2;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Issues the cp.async copies of chunk kc of tile (r0, s0) into buffer buf.
+template <int D>
+__device__ __forceinline__ void tc_load_chunk(const TcArgs& a, unsigned char* buf, int r0, int64_t s0, int kc,
+                                              int tid) {
+  constexpr int kABytes = kTcM * kTcKc * 2;
+  constexpr int kBBytes = kTcN * kTcKc * 2;
+  constexpr int kKg = kTcKc / 8;  // 16-byte groups along K
+  const int64_t n = a.st.n;
+  unsigned char* sA = buf;
+  unsigned char* sB = buf + kTcSlices * kABytes;
+  for (int v = tid; v < kTcSlices * kTcM * kKg; v += 256) {
+    const int s = v / (kTcM * kKg);
+    const int rem = v % (kTcM * kKg);
+    const int m = rem / kKg, kg = rem % kKg;
+    const __nv_bfloat16* src = a.sa + (static_cast<int64_t>(s) * D + r0 + m) * D + kc + kg * 8;
+    cp_async16(smem_addr(sA + s * kABytes + (m / 8) * (kKg * 128) + kg * 128 + (m % 8) * 16), src, true);
+  }
+  for (int v = tid; v < kTcSlices * kTcN * kKg; v += 256) {
+    const int s = v / (kTcN * kKg);
+    const int rem = v % (kTcN * kKg);
+    const int c = rem / kKg, kg = rem % kKg;
+    const int64_t sys = s0 + c;
+    const bool valid = sys < n;
+    const __nv_bfloat16* src = a.sy + (static_cast<int64_t>(s) * n + (valid ? sys : 0)) * D + kc + kg * 8;
+    cp_async16(smem_addr(sB + s * kBBytes + (c / 8) * (kKg * 128) + kg * 128 + (c % 8) * 16), src, valid);
+  }
+  cp_async_commit();
+}
+
 template <int D>
 __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  constexpr int kABytes = kTcM * kTcKc * 2;  // 16384
-  constexpr int kBBytes = kTcN * kTcKc * 2;  // 8192
-  unsigned char* sA = tc_smem;
-  unsigned char* sB = tc_smem + kTcSlices * kABytes;
-  __shared__ __align__(8) uint64_t mbar;
+  constexpr int kABytes = kTcM * kTcKc * 2;  // 8192
+  constexpr int kBBytes = kTcN * kTcKc * 2;  // 4096
+  constexpr int kChunks = D / kTcKc;
+  constexpr int kKg = kTcKc / 8;
+  static_assert(kChunks >= 2, "two-buffer pipeline needs two chunks");
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int any_running;
 
   const int tid = threadIdx.x;
   const int warp = tid / 32;
-  const int r0 = blockIdx.y * kTcM;
-  const int64_t s0 = static_cast<int64_t>(blockIdx.x) * kTcN;
   const int64_t n = a.st.n;
-
-  if (tid == 0) any_running = 0;
-  __syncthreads();
-  if (tid < kTcN && s0 + tid < n && a.st.status[s0 + tid] == kLinRunning) any_running = 1;
-  __syncthreads();
-  if (!any_running) return;
+  const int64_t ntx = (n + kTcN - 1) / kTcN;
+  const int64_t ntiles = ntx * (D / kTcM);
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_sh)),
@@ -148,91 +186,114 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
-  const uint32_t mb = smem_addr(&mbar);
-  uint32_t phase = 0;
+  uint32_t phase[2] = {0u, 0u};
   bool ok = true;
 
-  for (int kc = 0; kc < D; kc += kTcKc) {
-    // Stage the chunk: 16-byte vectors (8 bf16 along K) into core matrices.
-    for (int v = tid; v < kTcSlices * kTcM * (kTcKc / 8); v += 256) {
-      const int s = v / (kTcM * (kTcKc / 8));
-      const int rem = v % (kTcM * (kTcKc / 8));
-      const int m = rem / (kTcKc / 8), kg = rem % (kTcKc / 8);
-      const uint4 val = *reinterpret_cast<const uint4*>(
-          a.sa + (static_cast<int64_t>(s) * D + r0 + m) * D + kc + kg * 8);
-      *reinterpret_cast<uint4*>(sA + s * kABytes + (m / 8) * 1024 + kg * 128 + (m % 8) * 16) = val;
-    }
-    for (int v = tid; v < kTcSlices * kTcN * (kTcKc / 8); v += 256) {
-      const int s = v / (kTcN * (kTcKc / 8));
-      const int rem = v % (kTcN * (kTcKc / 8));
-      const int c = rem / (kTcKc / 8), kg = rem % (kTcKc / 8);
-      const int64_t sys = s0 + c;
-      uint4 val = make_uint4(0u, 0u, 0u, 0u);
-      if (sys < n) val = *reinterpret_cast<const uint4*>(a.sy + (static_cast<int64_t>(s) * n + sys) * D + kc + kg * 8);
-      *reinterpret_cast<uint4*>(sB + s * kBBytes + (c / 8) * 1024 + kg * 128 + (c % 8) * 16) = val;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int r0 = static_cast<int>(tile / ntx) * kTcM;
+    const int64_t s0 = (tile % ntx) * kTcN;
+    if (tid == 0) any_running = 0;
     __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      constexpr uint32_t idesc = tc_idesc();
+    if (tid < kTcN && s0 + tid < n && a.st.status[s0 + tid] == kLinRunning) any_running = 1;
+    __syncthreads();
+    if (!any_running) continue;
+
+    tc_load_chunk<D>(a, tc_smem, r0, s0, 0, tid);
+    for (int c = 0; c < kChunks; ++c) {
+      const int buf = c & 1;
+      if (c + 1 < kChunks) {
+        // buffer (c+1)&1 was read by the MMAs of chunk c-1: wait for them
+        if (c >= 1) {
+          if (ok && !mbar_wait_bounded(smem_addr(&mbar[buf ^ 1]), phase[buf ^ 1], a.error_flag)) ok = false;
+          phase[buf ^ 1] ^= 1u;
+        }
+        tc_load_chunk<D>(a, tc_smem + (buf ^ 1) * kTcBufBytes, r0, s0, (c + 1) * kTcKc, tid);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0 && ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        constexpr uint32_t idesc = tc_idesc();
+        unsigned char* sA = tc_smem + buf * kTcBufBytes;
+        unsigned char* sB = sA + kTcSlices * kABytes;
 #pragma unroll 1
-      for (int ks = 0; ks < kTcKc / 16; ++ks) {
-        for (int s = 0; s < kTcSlices; ++s) {
-          for (int t = 0; s + t < kTcSlices; ++t) {
-            const int d = s + t;
-            const uint64_t ad = umma_desc(smem_addr(sA + s * kABytes + ks * 256), 128, 1024);
-            const uint64_t bd = umma_desc(smem_addr(sB + t * kBBytes + ks * 256), 128, 1024);
-            // The first product into diagonal d is the pair (0, d) of the first
-            // K step: it overwrites the accumulator, every later one adds.
-            const uint32_t acc = (kc == 0 && ks == 0 && s == 0) ? 0u : 1u;
-            tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+        for (int ks = 0; ks < kTcKc / 16; ++ks) {
+          for (int s = 0; s < kTcSlices; ++s) {
+            for (int t = 0; s + t < kTcSlices; ++t) {
+              const int d = s + t;
+              const uint64_t ad = umma_desc(smem_addr(sA + s * kABytes + ks * 256), 128, kKg * 128);
+              const uint64_t bd = umma_desc(smem_addr(sB + t * kBBytes + ks * 256), 128, kKg * 128);
+              // The first product into diagonal d is the pair (0, d) of the
+              // first K step: it overwrites the accumulator, later ones add.
+              const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
+              tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+            }
           }
         }
+        tc_commit(smem_addr(&mbar[buf]));
       }
-      tc_commit(mb);
+      __syncthreads();
     }
-    if (!mbar_wait_bounded(mb, phase, a.error_flag)) ok = false;
-    phase ^= 1u;
+    // the last chunk's MMAs (and, through them, all earlier ones) are done
+    {
+      // (after a timeout no wait is attempted again: the kernel only frees
+      // its resources and returns)
+      const int last = (kChunks - 1) & 1;
+      if (ok && !mbar_wait_bounded(smem_addr(&mbar[last ^ 1]), phase[last ^ 1], a.error_flag)) ok = false;
+      phase[last ^ 1] ^= 1u;
+      if (ok && !mbar_wait_bounded(smem_addr(&mbar[last]), phase[last], a.error_flag)) ok = false;
+      phase[last] ^= 1u;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+      // Epilogue: warps 0..3 own TMEM lanes (rows) 32w..32w+31, warps 4..7
+      // the same rows for the second half of the 64 columns.
+      const int rw = warp % 4;
+      const int row = r0 + rw * 32 + (tid % 32);
+      const int cbase = (warp / 4) * 32;
+      const int erow = a.ea[row];
+      for (int cb = cbase; cb < cbase + 32; cb += 16) {
+        // Diagonal d holds an exact integer below 2^23 scaled by 2^(-6(d+2)):
+        // the sum over d is an exact 64-bit integer times 2^-42.
+        long long acc[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j] = 0;
+#pragma unroll
+        for (int d = 0; d < kTcSlices; ++d) {
+          float v[16];
+          tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cb), v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            acc[j] += static_cast<long long>(__float2int_rz(v[j])) << (kTcBits * (kTcSlices - 1 - d));
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t sys = s0 + cb + j;
+          if (sys >= n || a.st.status[sys] != kLinRunning) continue;
+          const int pe = erow + a.ey[sys] - kTcBits * (kTcSlices + 1);
+          const double p2 = (pe >= -1022 && pe <= 1023) ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
+                                                       : ldexp(1.0, pe);
+          a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = (__ll2double_rn(acc[j]) * p2) * a.st.dt[sys];
+        }
+      }
+    }
+    // TMEM is overwritten by the next tile's first MMA
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (!ok) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-
-  // Epilogue: warps 0..3 own TMEM lanes (rows) 32w..32w+31, warps 4..7 the
-  // same rows for the second half of the 64 columns.
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
-    const int rw = warp % 4;
-    const int row = r0 + rw * 32 + (tid % 32);
-    const int cbase = (warp / 4) * 32;
-    const int erow = a.ea[row];
-    for (int cb = cbase; cb < cbase + 32; cb += 16) {
-      double accd[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) accd[j] = 0.0;
-      for (int d = kTcSlices - 1; d >= 0; --d) {
-        float v[16];
-        tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cb), v);
-        const double scale = ldexp(1.0, -kTcBits * (d + 2));
-#pragma unroll
-        for (int j = 0; j < 16; ++j) accd[j] = fma(static_cast<double>(v[j]), scale, accd[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int64_t sys = s0 + cb + j;
-        if (sys >= n || a.st.status[sys] != kLinRunning) continue;
-        const double f = ldexp(accd[j], erow + a.ey[sys]);
-        a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = f * a.st.dt[sys];
-      }
-    }
-  }
+  cp_async_wait<0>();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -240,8 +301,40 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
   }
 }
 
-// Slices of the stage inputs Y_i = y + sum_j M(i,j) K_j, one warp per system:
-// exponent e with max|Y| < 2^e, then q_s = trunc(Y * 2^(6(s+1) - e) - carried).
+// Integer slicing.  With e the exponent of the largest |x| of a row (or a
+// system), |x| / 2^e < 1 and its first 36 fraction bits, F = floor(|x| *
+// 2^(36-e)), are the mantissa shifted right; slice s is bits 35-6s..30-6s of
+// F with the sign of x.  This equals truncating 64 r, r -= trunc, six times in
+// FP64 (every step of that is exact), without the FP64 instructions GB300
+// runs at 1/64 of its integer rate.  Returns e for the largest magnitude bits.
+__device__ __forceinline__ int tc_exponent_of(unsigned long long max_abs_bits) {
+  // max_abs_bits = bits of the largest |x|; e with |x| < 2^e, 0 for zero
+  if (max_abs_bits == 0ull) return 0;
+  const int ex = static_cast<int>(max_abs_bits >> 52);
+  if (ex == 0) return -1010 - __clzll(static_cast<long long>(max_abs_bits));  // subnormal: top bit p, 2^(p-1074)
+  return ex - 1022;  // |x| in [2^(ex-1023), 2^(ex-1022))
+}
+
+__device__ __forceinline__ void tc_slices(double x, int e, __nv_bfloat16 (&q)[kTcSlices]) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int ex = static_cast<int>((b >> 52) & 0x7ff);
+  const unsigned long long m = (b & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
+  // |x| = m * 2^(ex' - 1075) with ex' = max(ex, 1); F = m * 2^(ex' - 1075 + 36 - e)
+  const int sh = 1075 - 36 + e - (ex ? ex : 1);  // right shift, >= 17 since |x| < 2^e
+  const unsigned long long F = sh >= 64 ? 0ull : (m >> sh);
+  const bool neg = (b >> 63) != 0ull;
+#pragma unroll
+  for (int s = 0; s < kTcSlices; ++s) {
+    const int v = static_cast<int>((F >> (30 - 6 * s)) & 63ull);
+    q[s] = __float2bfloat16_rz(static_cast<float>(neg ? -v : v));
+  }
+}
+
+__device__ __forceinline__ unsigned long long tc_abs_bits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffull;
+}
+
+// Slices of the stage inputs Y_i = y + sum_j M(i,j) K_j, one warp per system.
 template <class Tab, int D, int STAGE>
 __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_bfloat16* sy, int32_t* ey) {
   constexpr int PER = D / 32;
@@ -250,7 +343,7 @@ __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_
   const int64_t n = a.st.n;
   if (sys >= n || a.st.status[sys] != kLinRunning) return;
   double v[PER];
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int64_t off = sys * D + lane + 32 * q;
@@ -261,25 +354,22 @@ __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_
       if constexpr (m != 0.0) x = fma(a.st.K[(static_cast<int64_t>(j) * n) * D + off], m, x);
     });
     v[q] = x;
-    mx = fmax(mx, fabs(x));
+    const unsigned long long ab = tc_abs_bits(x);
+    mx = ab > mx ? ab : mx;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx > 0.0) {
-    frexp(mx, &e);  // mx < 2^e
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = other > mx ? other : mx;
   }
+  const int e = tc_exponent_of(mx);
   if (lane == 0) ey[sys] = e;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
-    double r = ldexp(v[q], -e);  // |r| < 1
+    __nv_bfloat16 qs[kTcSlices];
+    tc_slices(v[q], e, qs);
 #pragma unroll
-    for (int s = 0; s < kTcSlices; ++s) {
-      r = ldexp(r, kTcBits);
-      const double qs = trunc(r);
-      r -= qs;
-      sy[(static_cast<int64_t>(s) * n + sys) * D + lane + 32 * q] = __double2bfloat16(qs);
-    }
+    for (int s = 0; s < kTcSlices; ++s) sy[(static_cast<int64_t>(s) * n + sys) * D + lane + 32 * q] = qs[s];
   }
 }
 
@@ -290,27 +380,27 @@ __global__ void __launch_bounds__(256) lin_tc_slice_a_kernel(const double* A, __
   const unsigned lane = threadIdx.x & 31u;
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   if (row >= D) return;
-  double v[PER], mx = 0.0;
+  double v[PER];
+  unsigned long long mx = 0ull;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     v[q] = A[static_cast<int64_t>(row) * D + lane + 32 * q];
-    mx = fmax(mx, fabs(v[q]));
+    const unsigned long long ab = tc_abs_bits(v[q]);
+    mx = ab > mx ? ab : mx;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = other > mx ? other : mx;
+  }
+  const int e = tc_exponent_of(mx);
   if (lane == 0) ea[row] = e;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
-    double r = ldexp(v[q], -e);
+    __nv_bfloat16 qs[kTcSlices];
+    tc_slices(v[q], e, qs);
 #pragma unroll
-    for (int s = 0; s < kTcSlices; ++s) {
-      r = ldexp(r, kTcBits);
-      const double qs = trunc(r);
-      r -= qs;
-      sa[(static_cast<int64_t>(s) * D + row) * D + lane + 32 * q] = __double2bfloat16(qs);
-    }
+    for (int s = 0; s < kTcSlices; ++s) sa[(static_cast<int64_t>(s) * D + row) * D + lane + 32 * q] = qs[s];
   }
 }
 

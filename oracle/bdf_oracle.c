@@ -392,6 +392,7 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
   static __thread double J[ORC_MAX_BDF_DIM * ORC_MAX_BDF_DIM];
   static __thread dmat M;
   double c[ORC_MAX_BDF_DIM], f[ORC_MAX_BDF_DIM], g[ORC_MAX_BDF_DIM], dx[ORC_MAX_BDF_DIM];
+  double rinv[ORC_MAX_BDF_DIM]; /* 1 / U[i][i], the elimination's own reciprocal */
   int piv[ORC_MAX_BDF_DIM];
   const double hb = dt * kBdfB[q];
   /* constant part c = sum_j a_j H[j-1] */
@@ -413,6 +414,7 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
       for (int k = 0; k < n; ++k) { const double t = M[i][k]; M[i][k] = M[pr][k]; M[pr][k] = t; }
     if (M[i][i] == 0.0) return 0;
     const double inv = 1.0 / M[i][i];
+    rinv[i] = inv;
     for (int r = i + 1; r < n; ++r) {
       const double l = M[r][i] * inv;
       M[r][i] = l;
@@ -429,8 +431,10 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
       if (piv[i] != i) { const double t = dx[i]; dx[i] = dx[piv[i]]; dx[piv[i]] = t; }
     for (int i = 0; i < n; ++i)
       for (int r = i + 1; r < n; ++r) dx[r] = dx[r] - (M[r][i] * dx[i]);
+    /* back substitution multiplies by the reciprocal the elimination formed
+     * (no division on the solve's critical path) */
     for (int i = n - 1; i >= 0; --i) {
-      dx[i] = dx[i] / M[i][i];
+      dx[i] = dx[i] * rinv[i];
       for (int r = 0; r < i; ++r) dx[r] = dx[r] - (M[r][i] * dx[i]);
     }
     double dn = 0.0;
