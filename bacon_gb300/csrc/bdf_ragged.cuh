@@ -1,45 +1,49 @@
-// Corrected BDF for batches whose systems differ in size: one warp per system.
+// Corrected BDF for batches whose systems differ in size: a group of warps
+// per system, one row per thread.
 //
 // A damped spring-mass chain of N_i masses (dim 2 N_i, up to 128) is too big
-// for one thread's registers, so one warp owns one system: lane l owns rows
-// l, l+32, l+64, l+96 of every vector.  Everything the warp touches in its
-// inner loops lives in its slice of shared memory: the LU factors of
-// M = I - h b_q J in use (column-major, so lane r reads row r of a column
-// without bank conflicts), their row permutation, the history H[0..6], the
-// interpolated history HH, a staging vector and the parameters.
+// for one thread's registers.  A group of G = ceil(dim / 32) warps owns one
+// system: thread r of the group owns row r of every vector.  Everything the
+// group's inner loops touch lives in its slice of shared memory: the LU
+// factors of M = I - h b_q J in use (column-major: a column is one
+// conflict-free read across the group), the pivot reciprocals and the row
+// permutation, the history H[0..6], the interpolated history HH, a staging
+// vector, the parameters and a small exchange area for broadcasts and
+// reductions.  The substitutions are a dependent chain over the pivots: the
+// owner of row i publishes x_i (a shuffle within one warp, else a shared-
+// memory slot and the group's named barrier) and every other row updates
+// itself, so a large system keeps G warps issuing instead of one warp running
+// G rows per lane.
 //
 // Factors are costly to recompute (2/3 dim^3 flops) and the chain Jacobian is
 // constant, so M depends on h b_q alone.  A solve meets ~100 distinct values
 // of h b_q (h moves by factors of 2, q ramps 1..6 after every doubling) and
 // revisits them constantly (orders q and q-1 alternate within every step).
-// Each warp therefore keeps a 16-entry least-recently-used cache of factor
+// Each group therefore keeps a 16-entry least-recently-used cache of factor
 // sets in device memory, keyed by the bits of h b_q: a hit copies the factors
 // into shared memory, a miss factors in shared memory and writes them back.
 // Reusing a factorisation of the same matrix is bit-identical to redoing it.
 //
-// Occupancy follows size.  GB300 issues one FP64 warp instruction every 16
-// cycles per SM, so one warp with four independent row updates per pivot
-// keeps the FP64 pipe busy at dim 128, while small systems need many warps to
-// cover shuffle and shared-memory latency.  A CTA of 8 warps and ~206 KB of
-// shared memory runs four phases, one per size class (dim <= 128, 96, 64, 32),
-// with 1, 2, 5 and 8 warps working; each class has its own work counter and
-// largest-first order, and a CTA moves to the next class when the counter of
-// the current one runs out.  The uniform part of a mixed batch (one thread per
-// system) runs after the last phase on all 8 warps.
+// A CTA of 8 warps (one per SM: its shared memory fills the SM) runs four
+// phases, one per size class: dim <= 128 (one group of 4 warps), <= 96 (two
+// groups of 3), <= 64 (four of 2), <= 32 (eight of 1).  Each class has its own
+// work counter and largest-first order; a CTA moves to the next class when
+// the counter of the current one runs out.  The uniform part of a mixed batch
+// (one thread per system) runs after the last phase on all 8 warps.
 //
 // Every floating-point operation is the one-thread corrected BDF's
 // (bdf_corrected_system, and the CPU oracle's bdf_corrected) on the same
 // operands in the same order, so the results are bit-identical to them:
-//   - partial-pivot LU: pivot = first row of maximum |M[r][i]| (a warp
+//   - partial-pivot LU: pivot = first row of maximum |M[r][i]| (a group
 //     arg-max with lowest-index ties), whole-row swaps, l = M[r][i] * (1 /
 //     M[i][i]), M[r][k] -= l M[i][k] row by row and pivot by pivot;
 //   - substitutions: row r receives its updates in pivot order, the back
 //     substitution multiplies by the pivot reciprocals the elimination
-//     formed (no division on its critical path); the permutation is applied
-//     as one gather (it only moves values);
+//     formed; the permutation is applied as one gather (it only moves
+//     values);
 //   - the Newton step norm and the error norm only feed comparisons with
-//     thresholds: a warp tree sum decides them unless it lies within 1e-10
-//     of a threshold, where the oracle's ordered sum on one lane decides.
+//     thresholds: a group tree sum decides them unless it lies within 1e-10
+//     of a threshold, where the oracle's ordered sum on one thread decides.
 #pragma once
 
 #include <type_traits>
@@ -49,22 +53,22 @@
 namespace bacon {
 
 constexpr int kRagMaxDim = 128;
-constexpr int kRagChunks = kRagMaxDim / 32;  // rows per lane
-constexpr int kRagWarps = 8;                 // warps per CTA
+constexpr int kRagWarps = 8;  // warps per CTA
 constexpr int kRagClasses = 4;
 constexpr int kRagCacheSlots = 16;
 
-// Size classes: the largest dim of the class and the warps of its phase.
+// Size classes: the largest dim, the warps of one group (one row per
+// thread) and the groups a CTA runs at a time.
 __host__ __device__ constexpr int rag_class_dim(int c) { return c == 0 ? 128 : c == 1 ? 96 : c == 2 ? 64 : 32; }
-__host__ __device__ constexpr int rag_class_warps(int c) { return c == 0 ? 1 : c == 1 ? 2 : c == 2 ? 5 : 8; }
+__host__ __device__ constexpr int rag_class_gwarps(int c) { return c == 0 ? 4 : c == 1 ? 3 : c == 2 ? 2 : 1; }
+__host__ __device__ constexpr int rag_class_groups(int c) { return c == 0 ? 1 : c == 1 ? 2 : c == 2 ? 4 : 8; }
 __host__ __device__ constexpr int rag_class_of(int dim) { return dim > 96 ? 0 : dim > 64 ? 1 : dim > 32 ? 2 : 3; }
-// The largest dim warp w of a CTA ever works on (the first class it joins).
-__host__ __device__ constexpr int rag_warp_max_dim(int w) { return w == 0 ? 128 : w == 1 ? 96 : w < 5 ? 64 : 32; }
 
-// One warp's shared-memory slice for systems of dim <= ld, in doubles:
+// One group's shared-memory slice for systems of dim <= ld, in doubles:
 // factors ld*ld, pivot reciprocals ld, H 7*ld, HH 7*ld, staging ld, params
 // ld/2+2, permutation ld/2 (ld ints), cache table 48 (16 keys, 16 stamps,
-// 16 states).
+// 16 states), exchange area 16 (2 broadcast slots, 2 x 4 reduction values,
+// 2 x 4 reduction indices).
 struct RagSmem {
   __host__ __device__ static constexpr int M(int) { return 0; }
   __host__ __device__ static constexpr int rinv(int ld) { return ld * ld; }
@@ -74,7 +78,8 @@ struct RagSmem {
   __host__ __device__ static constexpr int sp(int ld) { return ld * ld + 16 * ld; }
   __host__ __device__ static constexpr int perm(int ld) { return ld * ld + 16 * ld + ld / 2 + 2; }
   __host__ __device__ static constexpr int table(int ld) { return perm(ld) + ld / 2; }
-  __host__ __device__ static constexpr int doubles(int ld) { return table(ld) + 48; }
+  __host__ __device__ static constexpr int xch(int ld) { return table(ld) + 48; }
+  __host__ __device__ static constexpr int doubles(int ld) { return xch(ld) + 16; }
 };
 
 // Shared memory of a CTA for the classes present (bit c of mask = class c).
@@ -82,27 +87,25 @@ __host__ __device__ constexpr size_t rag_cta_smem_bytes(unsigned mask) {
   size_t b = 0;
   for (int c = 0; c < kRagClasses; ++c)
     if (mask & (1u << c)) {
-      const size_t need = static_cast<size_t>(rag_class_warps(c)) * RagSmem::doubles(rag_class_dim(c)) * 8;
+      const size_t need = static_cast<size_t>(rag_class_groups(c)) * RagSmem::doubles(rag_class_dim(c)) * 8;
       if (need > b) b = need;
     }
   return b;
 }
 
-// Device-memory factor cache of warp w: 16 slots of ld*ld factors, ld pivot
-// reciprocals and ld permutation ints, ld = rag_warp_max_dim(w); a CTA's
-// warps are laid out back to back.
+// Device-memory factor cache of one group: 16 slots of ld*ld factors, ld
+// pivot reciprocals and ld permutation ints.  A CTA's phases run one after
+// another, so they share one region sized for the largest phase.
 __host__ __device__ constexpr size_t rag_gslot_doubles(int ld) { return static_cast<size_t>(ld) * ld + ld + ld / 2; }
-__host__ __device__ constexpr size_t rag_gcache_warp_doubles(int w) {
-  return kRagCacheSlots * rag_gslot_doubles(rag_warp_max_dim(w));
+__host__ __device__ constexpr size_t rag_gcache_group_doubles(int c) {
+  return kRagCacheSlots * rag_gslot_doubles(rag_class_dim(c));
 }
 __host__ __device__ constexpr size_t rag_gcache_cta_doubles() {
   size_t s = 0;
-  for (int w = 0; w < kRagWarps; ++w) s += rag_gcache_warp_doubles(w);
-  return s;
-}
-__host__ __device__ constexpr size_t rag_gcache_warp_offset(int w) {
-  size_t s = 0;
-  for (int i = 0; i < w; ++i) s += rag_gcache_warp_doubles(i);
+  for (int c = 0; c < kRagClasses; ++c) {
+    const size_t need = rag_class_groups(c) * rag_gcache_group_doubles(c);
+    if (need > s) s = need;
+  }
   return s;
 }
 
@@ -160,123 +163,160 @@ struct RagChain {
   }
 };
 
+// The threads that own one system: thread t owns row t.  Synchronisation is
+// __syncwarp for a one-warp group, else the group's own named barrier.
+struct RagGroup {
+  int t;         // thread (= row) index in the group
+  int nthr;      // 32 * warps
+  int bar;       // named barrier id
+  double* xch;   // exchange area (RagSmem::xch)
+  int par;       // parity of the next reduction's buffer
+
+  __device__ __forceinline__ void sync() const {
+    if (nthr == 32) __syncwarp();
+    else __barrier_sync_count(static_cast<unsigned>(bar), static_cast<unsigned>(nthr));
+  }
+  // value of thread src, to every thread; slot alternates with the caller's
+  // step parity so that one barrier per broadcast suffices
+  __device__ __forceinline__ double bcast(double v, int src, int slot) const {
+    if (nthr == 32) return __shfl_sync(0xffffffffu, v, src);
+    if (t == src) xch[slot & 1] = v;
+    sync();
+    return xch[slot & 1];
+  }
+  // sum over the group in a fixed order (warp trees, then warps in order)
+  __device__ __forceinline__ double sum(double v) {
+    using O = ExactOps;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = O::add(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (nthr == 32) return v;
+    double* red = xch + 2 + 4 * par;
+    if ((t & 31) == 0) red[t >> 5] = v;
+    par ^= 1;
+    sync();
+    double s = red[0];
+    for (int w = 1; w < nthr / 32; ++w) s = O::add(s, red[w]);
+    return s;
+  }
+  // arg-max of (value, index) with the lowest index winning ties; NaN values
+  // never win
+  __device__ __forceinline__ int argmax(double v, int idx) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
+      if (ov > v || (ov == v && oi < idx)) {
+        v = ov;
+        idx = oi;
+      }
+    }
+    if (nthr == 32) return idx;
+    double* red = xch + 2 + 4 * par;
+    int* redi = reinterpret_cast<int*>(xch + 10) + 4 * par;
+    if ((t & 31) == 0) {
+      red[t >> 5] = v;
+      redi[t >> 5] = idx;
+    }
+    par ^= 1;
+    sync();
+    double bv = red[0];
+    int bi = redi[0];
+    for (int w = 1; w < nthr / 32; ++w)
+      if (red[w] > bv || (red[w] == bv && redi[w] < bi)) {
+        bv = red[w];
+        bi = redi[w];
+      }
+    return bi;
+  }
+};
+
 // M = I - hb J, then the partial-pivot LU in place (shared memory);
 // perm[pos] = the original row now at pos, rinv[i] = 1 / U[i][i] (the
 // elimination's own reciprocal, used again by the back substitution).
 // Returns false on an exactly zero pivot.
-__device__ __forceinline__ bool rag_factor(int lane, int D, int N, const double* sp, double hb, double* M,
+__device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const double* sp, double hb, double* M,
                                            double* rinv, int32_t* perm) {
   using O = ExactOps;
-  for (int k = 0; k < D; ++k)
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      if (r < D) M[k * D + r] = O::sub((r == k) ? 1.0 : 0.0, O::mul(hb, RagChain::jac(r, k, N, sp)));
-    }
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    if (r < D) perm[r] = r;
+  const int r = g.t;
+  if (r < D) {
+    for (int k = 0; k < D; ++k) M[k * D + r] = O::sub((r == k) ? 1.0 : 0.0, O::mul(hb, RagChain::jac(r, k, N, sp)));
+    perm[r] = r;
   }
-  __syncwarp();
+  g.sync();
   for (int i = 0; i < D; ++i) {
     double* col = M + i * D;
     const double diag = fabs(col[i]);
     int pr = i;
     if (diag == diag) {
-      double bv = diag;
-      int br = i;
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r > i && r < D) {
-          const double v = fabs(col[r]);
-          if (v > bv) {
-            bv = v;
-            br = r;
-          }
+      double v = diag;
+      int idx = i;
+      if (r > i && r < D) {
+        const double a = fabs(col[r]);
+        if (a > diag) {
+          v = a;
+          idx = r;
         }
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, bv, off);
-        const int orr = __shfl_xor_sync(0xffffffffu, br, off);
-        if (ov > bv || (ov == bv && orr < br)) {
-          bv = ov;
-          br = orr;
-        }
-      }
-      pr = br;
+      pr = g.argmax(v, idx);
     }
     if (pr != i) {
-      for (int k = lane; k < D; k += 32) {
+      for (int k = r; k < D; k += g.nthr) {
         const double a = M[k * D + i];
         M[k * D + i] = M[k * D + pr];
         M[k * D + pr] = a;
       }
-      if (lane == 0) {
+      if (r == 0) {
         const int32_t a = perm[i];
         perm[i] = perm[pr];
         perm[pr] = a;
       }
-      __syncwarp();
+      g.sync();
     }
     const double piv = col[i];
     if (piv == 0.0) return false;
     const double inv = O::div(1.0, piv);
-    if (lane == 0) rinv[i] = inv;
-    double l[kRagChunks];
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      l[j] = 0.0;
-      if (r > i && r < D) {
-        l[j] = O::mul(col[r], inv);
-        col[r] = l[j];
+    if (r == 0) rinv[i] = inv;
+    if (r > i && r < D) {
+      const double l = O::mul(col[r], inv);
+      col[r] = l;
+      for (int k = i + 1; k < D; ++k) {
+        double* ck = M + k * D;
+        ck[r] = O::sub(ck[r], O::mul(l, ck[i]));
       }
     }
-    for (int k = i + 1; k < D; ++k) {
-      double* ck = M + k * D;
-      const double mik = ck[i];
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r > i && r < D) ck[r] = O::sub(ck[r], O::mul(l[j], mik));
-      }
-    }
-    __syncwarp();
+    g.sync();
   }
   return true;
 }
 
-// Warp copy of n doubles (n even; both pointers 16-byte aligned).
-__device__ __forceinline__ void rag_copy(int lane, double* dst, const double* src, int n) {
+// Group copy of n doubles (n even; both pointers 16-byte aligned).
+__device__ __forceinline__ void rag_copy(const RagGroup& g, double* dst, const double* src, int n) {
   const double2* s = reinterpret_cast<const double2*>(src);
   double2* d = reinterpret_cast<double2*>(dst);
-  const int n2 = n / 2;
-  int i = lane;
-  for (; i + 96 < n2; i += 128) {
-    const double2 a = s[i], b = s[i + 32], c = s[i + 64], e = s[i + 96];
+  const int n2 = n / 2, st = g.nthr;
+  int i = g.t;
+  for (; i + 3 * st < n2; i += 4 * st) {
+    const double2 a = s[i], b = s[i + st], c = s[i + 2 * st], e = s[i + 3 * st];
     d[i] = a;
-    d[i + 32] = b;
-    d[i + 64] = c;
-    d[i + 96] = e;
+    d[i + st] = b;
+    d[i + 2 * st] = c;
+    d[i + 3 * st] = e;
   }
-  for (; i < n2; i += 32) d[i] = s[i];
+  for (; i < n2; i += st) d[i] = s[i];
 }
 
-// The factor cache of one warp: shared-memory table of 16 (key, stamp,
-// state) entries for the device-memory slots, plus the key and state of the
-// factors currently in shared memory.
+// The factors currently in shared memory (their key and state: 0 none,
+// 1 factored, 2 singular) and the cache clock.  The device-memory slots are
+// described by a shared-memory table of 16 (key, stamp, state) entries.
 struct RagCache {
   long long cur_key;
-  int cur_state;  // 0 none, 1 factored, 2 singular
+  int cur_state;
   int clock;
 };
 
 // Makes the factors of M(hb) current in shared memory; returns 1 (factored)
 // or 2 (singular).
-__device__ __forceinline__ int rag_get_factors(int lane, int D, int N, const double* sp, double hb, double* sM,
+__device__ __forceinline__ int rag_get_factors(RagGroup& g, int D, int N, const double* sp, double hb, double* sM,
                                                double* srinv, int32_t* sperm, double* table, double* gcache,
                                                int gld, RagCache& cache) {
   const long long key = __double_as_longlong(hb);
@@ -292,15 +332,15 @@ __device__ __forceinline__ int rag_get_factors(int lane, int D, int N, const dou
   if (hit >= 0) {
     const int st = states[hit];
     if (st == 1) {
-      const double* g = gcache + hit * slot_doubles;
-      rag_copy(lane, sM, g, D * D);
-      rag_copy(lane, srinv, g + static_cast<size_t>(gld) * gld, D);
-      const int32_t* gp = reinterpret_cast<const int32_t*>(g + static_cast<size_t>(gld) * gld + gld);
-      for (int r = lane; r < D; r += 32) sperm[r] = gp[r];
+      const double* gs = gcache + hit * slot_doubles;
+      rag_copy(g, sM, gs, D * D);
+      rag_copy(g, srinv, gs + static_cast<size_t>(gld) * gld, D);
+      const int32_t* gp = reinterpret_cast<const int32_t*>(gs + static_cast<size_t>(gld) * gld + gld);
+      for (int r = g.t; r < D; r += g.nthr) sperm[r] = gp[r];
     }
-    __syncwarp();
-    if (lane == 0) stamps[hit] = cache.clock;
-    __syncwarp();
+    g.sync();
+    if (g.t == 0) stamps[hit] = cache.clock;
+    g.sync();
     cache.cur_key = key;
     cache.cur_state = st;
     return st;
@@ -314,161 +354,103 @@ __device__ __forceinline__ int rag_get_factors(int lane, int D, int N, const dou
     for (int s = 1; s < kRagCacheSlots; ++s)
       if (stamps[s] < stamps[victim]) victim = s;
   }
-  const int st = rag_factor(lane, D, N, sp, hb, sM, srinv, sperm) ? 1 : 2;
-  __syncwarp();
+  const int st = rag_factor(g, D, N, sp, hb, sM, srinv, sperm) ? 1 : 2;
+  g.sync();
   if (st == 1) {
-    double* g = gcache + victim * slot_doubles;
-    rag_copy(lane, g, sM, D * D);
-    rag_copy(lane, g + static_cast<size_t>(gld) * gld, srinv, D);
-    int32_t* gp = reinterpret_cast<int32_t*>(g + static_cast<size_t>(gld) * gld + gld);
-    for (int r = lane; r < D; r += 32) gp[r] = sperm[r];
+    double* gs = gcache + victim * slot_doubles;
+    rag_copy(g, gs, sM, D * D);
+    rag_copy(g, gs + static_cast<size_t>(gld) * gld, srinv, D);
+    int32_t* gp = reinterpret_cast<int32_t*>(gs + static_cast<size_t>(gld) * gld + gld);
+    for (int r = g.t; r < D; r += g.nthr) gp[r] = sperm[r];
   }
-  if (lane == 0) {
+  if (g.t == 0) {
     keys[victim] = key;
     stamps[victim] = cache.clock;
     states[victim] = st;
   }
-  __syncwarp();
+  g.sync();
   cache.cur_key = key;
   cache.cur_state = st;
   return st;
 }
 
 // Newton solve of y - hb f(y) + sum_j a_{q,j} HH[j-1] = 0 from the guess in
-// y (own rows), with the factors of M for hb.
-__device__ __forceinline__ bool rag_newton(int lane, int D, int N, const double* sp, double* sv, const double* HH,
+// y (this thread's row), with the factors of M for hb.
+__device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const double* sp, double* sv, const double* HH,
                                            int ld, int q, double h, double* sM, double* srinv, int32_t* sperm,
                                            double* table, double* gcache, int gld, RagCache& cache,
-                                           int max_newton, double tol, double (&y)[kRagChunks]) {
+                                           int max_newton, double tol, double& y) {
   using O = ExactOps;
+  const int r = g.t;
+  const bool own = r < D;
   const double hb = O::mul(h, bdf_b(q));
-  double c[kRagChunks];
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) c[j] = 0.0;
-  for (int jj = 1; jj <= q; ++jj) {
-    const double aj = bdf_a(q, jj);
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      if (r < D) c[j] = O::add(c[j], O::mul(aj, HH[(jj - 1) * ld + r]));
-    }
-  }
-  if (rag_get_factors(lane, D, N, sp, hb, sM, srinv, sperm, table, gcache, gld, cache) != 1) return false;
+  double c = 0.0;
+  if (own)
+    for (int jj = 1; jj <= q; ++jj) c = O::add(c, O::mul(bdf_a(q, jj), HH[(jj - 1) * ld + r]));
+  if (rag_get_factors(g, D, N, sp, hb, sM, srinv, sperm, table, gcache, gld, cache) != 1) return false;
   const double* M = sM;
-  int32_t src[kRagChunks];
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    src[j] = (r < D) ? sperm[r] : 0;
-  }
+  const int src = own ? sperm[r] : 0;
   const double conv = O::mul(1e-3, tol);
   for (int it = 0; it < max_newton; ++it) {
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      if (r < D) sv[r] = y[j];
-    }
-    __syncwarp();
-    double g[kRagChunks];
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      g[j] = 0.0;
-      if (r < D) g[j] = O::add(O::sub(y[j], O::mul(hb, RagChain::f(r, N, sv, sp))), c[j]);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      if (r < D) sv[r] = g[j];
-    }
-    __syncwarp();
-    double dx[kRagChunks];
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      dx[j] = (r < D) ? -sv[src[j]] : 0.0;
-    }
+    g.sync();
+    if (own) sv[r] = y;
+    g.sync();
+    const double gr = own ? O::add(O::sub(y, O::mul(hb, RagChain::f(r, N, sv, sp))), c) : 0.0;
+    g.sync();
+    if (own) sv[r] = gr;
+    g.sync();
+    double dx = own ? -sv[src] : 0.0;
     // forward substitution with the unit lower factor
-#pragma unroll
-    for (int jb = 0; jb < kRagChunks; ++jb) {
-      const int iend = min(32, D - 1 - 32 * jb);
-      for (int ii = 0; ii < iend; ++ii) {
-        const int i = 32 * jb + ii;
-        const double xi = __shfl_sync(0xffffffffu, dx[jb], ii);
-        const double* col = M + i * D;
-#pragma unroll
-        for (int j = jb; j < kRagChunks; ++j) {
-          const int r = lane + 32 * j;
-          if (r > i && r < D) dx[j] = O::sub(dx[j], O::mul(col[r], xi));
-        }
-      }
+    for (int i = 0; i + 1 < D; ++i) {
+      const double xi = g.bcast(dx, i, i);
+      if (r > i && own) dx = O::sub(dx, O::mul(M[i * D + r], xi));
     }
     // back substitution with the upper factor
-#pragma unroll
-    for (int jb = kRagChunks - 1; jb >= 0; --jb) {
-      const int ihi = min(31, D - 1 - 32 * jb);
-      for (int ii = ihi; ii >= 0; --ii) {
-        const int i = 32 * jb + ii;
-        const double* col = M + i * D;
-        if (static_cast<int>(lane) == ii) dx[jb] = O::mul(dx[jb], srinv[i]);
-        const double xi = __shfl_sync(0xffffffffu, dx[jb], ii);
-#pragma unroll
-        for (int j = 0; j <= jb; ++j) {
-          const int r = lane + 32 * j;
-          if (r < i) dx[j] = O::sub(dx[j], O::mul(col[r], xi));
-        }
-      }
+    for (int i = D - 1; i >= 0; --i) {
+      if (r == i) dx = O::mul(dx, srinv[i]);
+      const double xi = g.bcast(dx, i, i);
+      if (r < i) dx = O::sub(dx, O::mul(M[i * D + r], xi));
     }
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      if (r < D) {
-        y[j] = O::add(y[j], dx[j]);
-        sv[r] = dx[j];
-      }
+    if (own) {
+      y = O::add(y, dx);
+      sv[r] = dx;
     }
-    __syncwarp();
-    // ||dx||^2: the oracle sums it in order on one lane and tests
-    // sqrt(dn) <= conv.  A warp tree sum differs from that by ~dim * 2^-53
+    // ||dx||^2: the oracle sums it in order on one thread and tests
+    // sqrt(dn) <= conv.  The group tree sum differs from that by ~dim * 2^-53
     // (all terms are non-negative), so it decides alone unless it lies within
     // 1e-10 of conv^2; then the ordered sum decides.  NaN in either exactly
     // when some dx is NaN.
-    double part = 0.0;
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) part = O::add(part, O::mul(dx[j], dx[j]));
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) part = O::add(part, __shfl_xor_sync(0xffffffffu, part, off));
+    const double part = g.sum(own ? O::mul(dx, dx) : 0.0);
     if (!(part == part)) return false;
     const double thr = O::mul(conv, conv);
     if (fabs(O::sub(part, thr)) > O::mul(1e-10, thr)) {
       if (part < thr) return true;
       continue;
     }
+    g.sync();  // every row's dx is in sv
     double dn = 0.0;
-    if (lane == 0)
+    if (r == 0)
       for (int d = 0; d < D; ++d) dn = O::add(dn, O::mul(sv[d], sv[d]));
-    dn = __shfl_sync(0xffffffffu, dn, 0);
+    dn = g.bcast(dn, 0, 0);
+    g.sync();
     if (O::sqrt(dn) <= conv) return true;
   }
   return false;
 }
 
-// Euclidean norm of the vector in sv[0..D) in nalgebra's order for a
-// dynamically sized vector (eight partial sums, then the tail), warp-uniform.
-__device__ __forceinline__ double rag_norm(int lane, int D, const double* sv) {
+// Euclidean norm of sv[0..D) in nalgebra's order for a dynamically sized
+// vector (eight partial sums, then the tail); group-uniform.
+__device__ __forceinline__ double rag_norm(RagGroup& g, int D, const double* sv) {
   using O = ExactOps;
   double acc = 0.0;
   const int full = D - D % 8;
-  if (lane < 8)
-    for (int i = 0; i < full; i += 8) acc = O::add(acc, O::mul(sv[i + lane], sv[i + lane]));
+  if (g.t < 8)
+    for (int i = 0; i < full; i += 8) acc = O::add(acc, O::mul(sv[i + g.t], sv[i + g.t]));
   double a[8];
 #pragma unroll
   for (int l = 0; l < 8; ++l) a[l] = __shfl_sync(0xffffffffu, acc, l);
   double res = 0.0;
-  if (lane == 0) {
+  if (g.t == 0) {
     res = O::add(res, O::add(a[0], a[4]));
     res = O::add(res, O::add(a[1], a[5]));
     res = O::add(res, O::add(a[2], a[6]));
@@ -476,52 +458,41 @@ __device__ __forceinline__ double rag_norm(int lane, int D, const double* sv) {
     for (int k = full; k < D; ++k) res = O::add(res, O::mul(sv[k], sv[k]));
     res = O::sqrt(O::add(0.0, res));
   }
-  return __shfl_sync(0xffffffffu, res, 0);
+  res = g.bcast(res, 0, 1);
+  g.sync();
+  return res;
 }
 
 // A value that compares with tol and 0.1*tol exactly as rag_norm(sv) does:
-// the warp tree-sum norm (within ~dim * 2^-53 of the ordered one) unless it
+// the group tree-sum norm (within ~dim * 2^-53 of the ordered one) unless it
 // lies within 1e-10 of either threshold, else the ordered norm itself.
-__device__ __forceinline__ double rag_norm_decide(int lane, int D, const double* sv, double tol) {
+// sv must be written and synchronised by the caller.
+__device__ __forceinline__ double rag_norm_decide(RagGroup& g, int D, const double* sv, double tol) {
   using O = ExactOps;
-  double part = 0.0;
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    if (r < D) part = O::add(part, O::mul(sv[r], sv[r]));
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) part = O::add(part, __shfl_xor_sync(0xffffffffu, part, off));
-  const double e = O::sqrt(part);
+  const double v = g.t < D ? sv[g.t] : 0.0;
+  const double e = O::sqrt(g.sum(O::mul(v, v)));
   if (!(e == e)) return e;
   const double t2 = O::mul(0.1, tol);
   if (fabs(O::sub(e, tol)) > O::mul(1e-10, tol) && fabs(O::sub(e, t2)) > O::mul(1e-10, t2)) return e;
-  return rag_norm(lane, D, sv);
+  return rag_norm(g, D, sv);
 }
 
-// Interpolates the k history rows of this lane onto nodes -s*j (j < k).
-__device__ __forceinline__ void rag_interp_rows(int lane, int D, int ld, int k, double s, const double* src,
-                                                double* dst) {
+// Interpolates this thread's k history values onto nodes -s*j (j < k).
+__device__ __forceinline__ void rag_interp_row(int r, int ld, int k, double s, const double* src, double* dst) {
   using O = ExactOps;
   double w[7];
   for (int j = 0; j < k; ++j) {
     lagrange_weights(k - 1, O::mul(-s, static_cast<double>(j)), w);
-#pragma unroll
-    for (int jj = 0; jj < kRagChunks; ++jj) {
-      const int r = lane + 32 * jj;
-      if (r < D) {
-        double acc = 0.0;
-        for (int i = 0; i < k; ++i) acc = O::add(acc, O::mul(w[i], src[i * ld + r]));
-        dst[j * ld + r] = acc;
-      }
-    }
+    double acc = 0.0;
+    for (int i = 0; i < k; ++i) acc = O::add(acc, O::mul(w[i], src[i * ld + r]));
+    dst[j * ld + r] = acc;
   }
 }
 
-// One ragged system integrated by the calling warp; ws is its shared-memory
-// slice for dims <= ld, gcache its device-memory factor slots of dim <= gld.
-__device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t idx, int lane, double* ws, int ld,
-                                                 double* gcache, int gld) {
+// One ragged system integrated by the calling group; ws is its shared-memory
+// slice for dims <= ld, gcache its device-memory factor slots.
+__device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t idx, RagGroup& g, double* ws, int ld,
+                                                 double* gcache) {
   using O = ExactOps;
   double* sM = ws + RagSmem::M(ld);
   double* srinv = ws + RagSmem::rinv(ld);
@@ -531,25 +502,21 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
   double* sp = ws + RagSmem::sp(ld);
   int32_t* sperm = reinterpret_cast<int32_t*>(ws + RagSmem::perm(ld));
   double* table = ws + RagSmem::table(ld);
+  const int r = g.t;
   const int64_t yo = a.y_off[idx];
   const int D = static_cast<int>(a.y_off[idx + 1] - yo);
   const int N = D / 2;
+  const bool own = r < D;
   const int64_t po = a.p_off[idx];
-  __syncwarp();
-  for (int k = lane; k <= N; k += 32) sp[k] = a.params[po + k];
-  if (lane < 32) reinterpret_cast<int*>(table + 16)[lane] = 0;  // stamps and states of the 16 slots
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    if (r < D) H[r] = a.y0[yo + r];
+  g.sync();
+  for (int k = r; k <= N; k += g.nthr) sp[k] = a.params[po + k];
+  if (r < 32) reinterpret_cast<int*>(table + 16)[r] = 0;  // stamps and states of the 16 slots
+  double ly = 0.0;
+  if (own) {
+    ly = a.y0[yo + r];
+    H[r] = ly;
   }
-  double ly[kRagChunks];
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    ly[j] = (r < D) ? a.y0[yo + r] : 0.0;
-  }
-  __syncwarp();
+  g.sync();
   double dt_min = a.dt_min;
   const double dt_max = a.dt_max;
   if (dt_min > dt_max) dt_min = dt_max;
@@ -577,69 +544,45 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
     const int q = (k < qmax) ? k : qmax;
     const double* HHp = H;
     if (h != dt && k > 1) {
-      rag_interp_rows(lane, D, ld, k, O::div(h, dt), H, HH);
+      if (own) rag_interp_row(r, ld, k, O::div(h, dt), H, HH);
       HHp = HH;
     }
     // predictor: extrapolation through the history points
     double w[7];
     lagrange_weights(k - 1, 1.0, w);
-    double yh[kRagChunks], yl[kRagChunks];
-#pragma unroll
-    for (int j = 0; j < kRagChunks; ++j) {
-      const int r = lane + 32 * j;
-      double s = 0.0;
-      if (r < D)
-        for (int i = 0; i < k; ++i) s = O::add(s, O::mul(w[i], HHp[i * ld + r]));
-      yh[j] = s;
-    }
-    __syncwarp();
+    double yh = 0.0, yl = 0.0;
+    if (own)
+      for (int i = 0; i < k; ++i) yh = O::add(yh, O::mul(w[i], HHp[i * ld + r]));
     const double t1 = O::add(t, h);
-    bool ok = rag_newton(lane, D, N, sp, sv, HHp, ld, q, h, sM, srinv, sperm, table, gcache, gld, cache,
-                         a.max_iter, a.tol, yh);
+    bool ok = rag_newton(g, D, N, sp, sv, HHp, ld, q, h, sM, srinv, sperm, table, gcache, ld, cache, a.max_iter,
+                         a.tol, yh);
     double error;
     if (ok && q >= 2) {
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) yl[j] = yh[j];
-      ok = rag_newton(lane, D, N, sp, sv, HHp, ld, q - 1, h, sM, srinv, sperm, table, gcache, gld, cache,
-                      a.max_iter, a.tol, yl);
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r < D) sv[r] = O::sub(yh[j], yl[j]);
-      }
-      __syncwarp();
-      error = rag_norm_decide(lane, D, sv, a.tol);
+      yl = yh;
+      ok = rag_newton(g, D, N, sp, sv, HHp, ld, q - 1, h, sM, srinv, sperm, table, gcache, ld, cache, a.max_iter,
+                      a.tol, yl);
+      g.sync();
+      if (own) sv[r] = O::sub(yh, yl);
+      g.sync();
+      error = rag_norm_decide(g, D, sv, a.tol);
     } else {
       // order 1: half the gap between backward and forward Euler
-      double diff[kRagChunks];
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        diff[j] = 0.0;
-        if (r < D) diff[j] = O::mul(0.5, O::sub(yh[j], O::add(H[r], O::mul(h, RagChain::f(r, N, H, sp)))));
-      }
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r < D) sv[r] = diff[j];
-      }
-      __syncwarp();
-      error = rag_norm_decide(lane, D, sv, a.tol);
+      const double diff =
+          own ? O::mul(0.5, O::sub(yh, O::add(H[r], O::mul(h, RagChain::f(r, N, H, sp))))) : 0.0;
+      g.sync();
+      if (own) sv[r] = diff;
+      g.sync();
+      error = rag_norm_decide(g, D, sv, a.tol);
     }
     if (ok && error <= a.tol) {
       const int kk = (k < 7) ? k + 1 : 7;
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r < D) {
-          for (int i = kk - 1; i >= 1; --i) H[i * ld + r] = H[(i - 1) * ld + r];
-          H[r] = yh[j];
-          ly[j] = yh[j];
-        }
+      g.sync();  // every row has finished reading H
+      if (own) {
+        for (int i = kk - 1; i >= 1; --i) H[i * ld + r] = H[(i - 1) * ld + r];
+        H[r] = yh;
+        ly = yh;
       }
-      __syncwarp();
+      g.sync();
       k = kk;
       t = t1;
       ++acc;
@@ -647,13 +590,9 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
       if (h != dt) continue;
       if (error < O::mul(0.1, a.tol) && k == qmax + 1 && O::mul(dt, 2.0) <= dt_max) {
         const int nk = (k + 1) / 2;
-#pragma unroll
-        for (int j = 0; j < kRagChunks; ++j) {
-          const int r = lane + 32 * j;
-          if (r < D)
-            for (int i = 1; i < nk; ++i) H[i * ld + r] = H[2 * i * ld + r];
-        }
-        __syncwarp();
+        if (own)
+          for (int i = 1; i < nk; ++i) H[i * ld + r] = H[2 * i * ld + r];
+        g.sync();
         k = nk;
         dt = O::mul(dt, 2.0);
       }
@@ -666,59 +605,62 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
       break;
     }
     if (k > 1) {
-      rag_interp_rows(lane, D, ld, k, 0.5, H, HH);
-#pragma unroll
-      for (int j = 0; j < kRagChunks; ++j) {
-        const int r = lane + 32 * j;
-        if (r < D)
-          for (int i = 0; i < k; ++i) H[i * ld + r] = HH[i * ld + r];
+      g.sync();  // every row has finished reading H
+      if (own) {
+        rag_interp_row(r, ld, k, 0.5, H, HH);
+        for (int i = 0; i < k; ++i) H[i * ld + r] = HH[i * ld + r];
       }
-      __syncwarp();
+      g.sync();
     }
     dt = nd;
   }
-#pragma unroll
-  for (int j = 0; j < kRagChunks; ++j) {
-    const int r = lane + 32 * j;
-    if (r < D) a.y_out[yo + r] = ly[j];
-  }
-  if (lane == 0) {
+  if (own) a.y_out[yo + r] = ly;
+  if (r == 0) {
     a.t_out[idx] = last_t;
     a.accepted[idx] = acc;
     a.rejected[idx] = rej;
     a.status[idx] = status;
     if (status != kStOk) atomicMin(a.first_fail, static_cast<unsigned long long>(idx));
   }
-  __syncwarp();
+  g.sync();
 }
 
 // Marker for a mixed launch without a uniform (one-thread-per-system) part.
 struct NoSmall {};
 
-// One launch for a stiff batch of two parts: ragged systems (a warp each, in
-// four size-class phases) and a uniform batch of small systems (a thread
-// each, after the last phase).  Launched with kRagWarps * 32 threads and
-// rag_cta_smem_bytes(classes present) of dynamic shared memory.
+// One launch for a stiff batch of two parts: ragged systems (a group of
+// warps each, in four size-class phases) and a uniform batch of small systems
+// (a thread each, after the last phase).  Launched with kRagWarps * 32 threads
+// and rag_cta_smem_bytes(classes present) of dynamic shared memory.
 template <class Small>
 __global__ void __launch_bounds__(kRagWarps * 32, 1)
     bdf_mixed_kernel(const BdfArgs small, int small_dyn, const RaggedArgs rg) {
   extern __shared__ __align__(16) double rag_smem[];
   const int warp = static_cast<int>(threadIdx.x >> 5);
-  const int lane = static_cast<int>(threadIdx.x & 31u);
-  double* gcache = rg.gcache + static_cast<size_t>(blockIdx.x) * rag_gcache_cta_doubles() +
-                   rag_gcache_warp_offset(warp);
+  double* gcache_cta = rg.gcache + static_cast<size_t>(blockIdx.x) * rag_gcache_cta_doubles();
   for (int c = 0; c < kRagClasses; ++c) {
     if (rg.class_n[c] == 0) continue;
-    if (warp < rag_class_warps(c)) {
+    const int gw = rag_class_gwarps(c);
+    const int grp = warp / gw;
+    if (grp < rag_class_groups(c)) {
       const int ld = rag_class_dim(c);
-      double* ws = rag_smem + static_cast<size_t>(warp) * RagSmem::doubles(ld);
+      double* ws = rag_smem + static_cast<size_t>(grp) * RagSmem::doubles(ld);
+      RagGroup g;
+      g.t = static_cast<int>(threadIdx.x) - grp * gw * 32;
+      g.nthr = gw * 32;
+      g.bar = 1 + grp;
+      g.xch = ws + RagSmem::xch(ld);
+      g.par = 0;
+      double* gcache = gcache_cta + static_cast<size_t>(grp) * rag_gcache_group_doubles(c);
+      unsigned long long* slot = reinterpret_cast<unsigned long long*>(g.xch + 15);
       for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(rg.queues + c, 1ull);
-        item = __shfl_sync(0xffffffffu, item, 0);
+        if (g.t == 0) *slot = atomicAdd(rg.queues + c, 1ull);
+        g.sync();
+        const unsigned long long item = *slot;
+        g.sync();
         if (item >= static_cast<unsigned long long>(rg.class_n[c])) break;
         const int64_t idx = static_cast<int64_t>(rg.order[rg.class_start[c] + static_cast<int64_t>(item)]);
-        rag_solve_system(rg, idx, lane, ws, ld, gcache, rag_warp_max_dim(warp));
+        rag_solve_system(rg, idx, g, ws, ld, gcache);
       }
     }
     __syncthreads();

@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--n", type=int, default=1 << 20, help="systems per GPU")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="systems in the CPU sample")
     ap.add_argument("--skip-extras", action="store_true", help="skip plain/FMA/CPU side measurements")
+    ap.add_argument("--stiff-n", type=int, default=32768,
+                    help="systems of the stiff-batch side measurement (half Robertson, half chains); the "
+                         "workload's full size is 131072")
     ap.add_argument("--precision", default="fp64_exact", choices=["fp64_exact", "fp64_fma", "fp32_comp"],
                     help="arithmetic of the timed solve (the headline is fp64_exact)")
     return ap.parse_args()
@@ -150,6 +153,61 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def cpu_pool(fn, items, threads):
+    """Runs fn over items on `threads` host threads (the oracle's C calls drop
+    the GIL); returns (results, seconds)."""
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(fn, items))
+    return res, time.perf_counter() - t0
+
+
+def other_cpu_baselines(W):
+    """The CPU restatement timed on bounded samples of the other workloads, on
+    all host threads (reported baselines: the GPU numbers are measured on the
+    full workloads)."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    out = {}
+    vb = W.van_der_pol()
+    cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_QRT, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max)
+    r = O.rk_solve_batch(cfg, vb.rhs, vb.y0, vb.params, vb.t0, vb.t_end, threads=threads)
+    out["van_der_pol_4096"] = {"value": vb.n / r["seconds"], "unit": "solves/s", "cores": threads,
+                               "sample": "all 4096 systems"}
+    lb = W.linear_shared(n=2 * threads)
+    cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_QRT, tol=lb.tol, dt_min=lb.dt_min, dt_max=lb.dt_max)
+    r = O.rk_solve_batch(cfg, lb.rhs, lb.y0, np.zeros((0, lb.n)), lb.t0, lb.t_end, shared=lb.extra["A"],
+                         threads=threads)
+    out["linear_shared_A_256"] = {"value": lb.n / r["seconds"], "unit": "solves/s", "cores": threads,
+                                  "sample": f"{lb.n} of the 65536 states (same A)"}
+    lv = W.lotka_volterra(n=1 << 18)
+    idx = np.arange(0, lv.n, lv.n // (64 * threads))
+    cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_QRT, tol=lv.tol, dt_min=lv.dt_min, dt_max=lv.dt_max)
+    _, sec = cpu_pool(lambda i: O.rk_adjoint_one(cfg, lv.rhs, lv.y0[:, i], lv.params[:, i], 0.0, 15.0,
+                                                 lv.extra["target"][:, i]), idx, threads)
+    out["adjoint"] = {"value": len(idx) / sec, "unit": "grads/s", "cores": threads,
+                      "sample": f"{len(idx)} of the 262144 Lotka-Volterra systems"}
+    rob, ch = W.stiff_batch(131072)
+    k = 4 * threads
+    ri = np.linspace(0, rob.n - 1, k).astype(int)
+    ci = np.linspace(0, ch.n - 1, k).astype(int)
+    rcfg = O.bdf_cfg(mode=O.BDF_CORRECTED, tol=rob.tol, dt_min=rob.dt_min, dt_max=rob.dt_max)
+    ccfg = O.bdf_cfg(mode=O.BDF_CORRECTED, dyn_dim=True, tol=ch.tol, dt_min=ch.dt_min, dt_max=ch.dt_max)
+
+    def one(job):
+        kind, i = job
+        if kind == 0:
+            return O.bdf_solve_one(rcfg, rob.rhs, rob.y0[:, i], 0.0, 1e4, params=rob.params[:, i]).status
+        y0, p = ch.system(i)
+        return O.bdf_solve_one(ccfg, ch.rhs, y0, 0.0, 10.0, params=p).status
+
+    _, sec = cpu_pool(one, [(0, i) for i in ri] + [(1, i) for i in ci], threads)
+    out["bdf6_stiff"] = {"value": 2 * k / sec, "unit": "solves/s", "cores": threads,
+                         "sample": f"{k} Robertson + {k} chains (evenly spaced) of the 131072-system batch"}
+    return out
+
+
 def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
     """The other benchmark workloads, one timed solve each (device-resident)."""
     out = {}
@@ -209,6 +267,8 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
     ms = ctx.last_kernel_ms()
     out["bdf6_stiff"] = {
         "value": stiff_n / (ms * 1e-3), "unit": "solves/s", "n": stiff_n, "kernel_ms": ms, "wall_s": wall,
+        "sample": "full workload" if stiff_n == 131072 else
+                  f"{stiff_n} of the workload's 131072 systems, same generator and mix (--stiff-n 131072 for all)",
         "robertson": {"n": rob.n, "t_end": 1e4, "statuses_ok": bool((us.status == 0).all().item()),
                       "accepted_mean": float(us.accepted.double().mean().item())},
         "spring_chains": {"n": ch.n, "dims": "4..128 (m ~ U{2..64} masses)", "t_end": 10.0,
@@ -418,7 +478,7 @@ def main():
             "e2e_value": lv.n / adj_wall, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
             "record_forward_ms": rec_ms, "reverse_ms": rev_ms, "cost_vs_forward": adj_ms / fwd_ms,
             "max_rel_diff_vs_frozen_central_fd_h1e-6": fd_rel, "fd_sample": 16}
-        extras.update(other_workloads(E, W, ctx, dev, torch))
+        extras.update(other_workloads(E, W, ctx, dev, torch, stiff_n=args.stiff_n))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -448,6 +508,9 @@ def main():
             "sample": f"{s.n} of the {b.n} Lorenz systems (seeded subset), all host threads",
             "sample_bit_identical": bool(np.array_equal(r["y"], out["y"].cpu().numpy()[:, idx])
                                          and np.array_equal(r["accepted"], acc[idx]))}
+        for name, base in other_cpu_baselines(W).items():
+            if isinstance(line.get(name), dict):
+                line[name]["cpu_baseline"] = base
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
