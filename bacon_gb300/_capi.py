@@ -98,6 +98,16 @@ class BdfOptions(ctypes.Structure):
     ]
 
 
+class AdamsOptions(ctypes.Structure):
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("memory", ctypes.c_int32),
+        ("max_attempts", ctypes.c_int64),
+        ("block", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+    ]
+
+
 class RaggedProblem(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_int64),
@@ -154,6 +164,10 @@ SIGNATURES = {
     "bacon_rk_validate": (ctypes.c_int, [ctypes.POINTER(Problem)]),
     "bacon_bdf_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(BdfOptions),
                                        ctypes.POINTER(RkResult)]),
+    "bacon_adams_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(AdamsOptions),
+                                         ctypes.POINTER(RkResult)]),
+    "bacon_euler_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.c_double,
+                                         ctypes.POINTER(AdamsOptions), ctypes.POINTER(RkResult)]),
     "bacon_ragged_validate": (ctypes.c_int, [ctypes.POINTER(RaggedProblem)]),
     "bacon_bdf_solve_mixed": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RaggedProblem),
                                              ctypes.POINTER(BdfOptions), ctypes.POINTER(RkResult),

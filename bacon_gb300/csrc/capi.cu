@@ -13,6 +13,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include "adams.h"
+#include "adams_kernel.cuh"
 #include "bdf.h"
 #include "linear.cuh"
 #include "linear.h"
@@ -130,6 +132,7 @@ struct bacon_ctx {
   bool rev_valid = false;
   std::vector<bacon::AdjEntry> adjoint_kernels;
   std::vector<bacon::BdfEntry> bdf_kernels;
+  std::vector<bacon::AdamsEntry> adams_kernels;
   DevBuf adj_dt, adj_ck, adj_tgt, adj_loss, adj_gy, adj_gp;
   DevBuf lin_A, lin_y, lin_K, lin_t, lin_dt, lin_end, lin_att;
   DevBuf tc_sa, tc_ea, tc_sy, tc_ey;
@@ -891,6 +894,101 @@ extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon
 }
 
 // ---------------------------------------------------------------------------
+// Adams predictor-corrector and Euler: one system per thread.
+namespace {
+
+int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double euler_dt,
+                     const bacon_adams_options* opt, bacon_rk_result* r) {
+  int rc;
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (c->adams_kernels.empty()) c->adams_kernels = bacon::all_adams_kernels();
+  const void* fn = nullptr;
+  for (const auto& e : c->adams_kernels)
+    if (e.order == order && e.rhs == p->rhs && e.dim == p->dim) fn = e.fn;
+  if (!fn) return fail(BACON_UNSUPPORTED, "no Adams/Euler kernel for this (rhs, dim)");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  bacon::AdamsArgs a{};
+  a.n = p->n;
+  a.y0 = o.y0;
+  a.params = o.params;
+  a.t0 = o.t0;
+  a.t_end = o.t_end;
+  a.t0_s = p->t0_scalar;
+  a.t_end_s = p->t_end_scalar;
+  a.tol = p->tol;
+  a.dt_min = p->dt_min;
+  a.dt_max = p->dt_max;
+  a.euler_dt = euler_dt;
+  a.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  a.y_out = o.y_out;
+  a.t_out = o.t_out;
+  a.accepted = o.acc;
+  a.rejected = o.rej;
+  a.status = o.st;
+  a.traj_t = o.traj_t;
+  a.traj_y = o.traj_y;
+  a.traj_cap = o.traj_t ? r->traj_cap : 0;
+  a.dyn_dim = p->dyn_dim ? 1 : 0;
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+  const int block = opt->block > 0 ? opt->block : 128;
+  if (block % 32 != 0 || block > 128) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 128");
+  int max_bps = 0;
+  BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
+  if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : model_blocks_per_sm(p->n, c->num_sms, block, max_bps);
+  if (bps > max_bps) bps = max_bps;
+  long long grid = static_cast<long long>(c->num_sms) * bps;
+  const long long need = (p->n + block - 1) / block;
+  if (grid > need) grid = need;
+  if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+  void* args[] = {&a};
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, 0, c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  if (host && (rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+  c->launches += 1;
+  c->ev_valid = true;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  return batch_return_code(c, r, host, o);
+}
+
+}  // namespace
+
+extern "C" int bacon_adams_solve(bacon_ctx* c, const bacon_problem* p, const bacon_adams_options* opt,
+                                 bacon_rk_result* r) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if (opt->order != 5 && opt->order != 3) return fail(BACON_INVALID_ARGUMENT, "order must be 5 or 3");
+  return adams_like_solve(c, p, opt->order, 0.0, opt, r);
+}
+
+extern "C" int bacon_euler_solve(bacon_ctx* c, const bacon_problem* p, double dt, const bacon_adams_options* opt,
+                                 bacon_rk_result* r) {
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  if (!p) return fail(BACON_INVALID_ARGUMENT, "problem is NULL");
+  if (!(dt > 0.0)) return fail(BACON_TIME_DELTA_OOB, "dt <= 0");
+  // Euler ignores the tolerance and the dt bounds (src/ivp.rs:390-393):
+  // validate the rest with placeholders for them.
+  bacon_problem q = *p;
+  q.tol = 1.0;
+  q.dt_min = q.dt_max = dt;
+  int rc = bacon_rk_validate(&q);
+  if (rc != BACON_OK) return rc;
+  return adams_like_solve(c, &q, 1, dt, opt, r);
+}
+
+// ---------------------------------------------------------------------------
 // Mixed stiff batch: ragged systems (a warp each) and a uniform batch of
 // small systems (a thread each) in one launch of bdf_mixed_kernel.
 namespace {
@@ -1347,6 +1445,8 @@ struct bacon_builder {
   bool dyn = false;
   bool has_dt_max = false, has_dt_min = false, has_t0 = false, has_end = false, has_tol = false;
   double dt_max = 0, dt_min = 0, t0 = 0, t_end = 0, tol = 0;
+  bool has_euler_dt = false;  // Euler (kind 6): one step size
+  double euler_dt = 0;
   std::vector<double> y0;
   int64_t n = 0;
   bool has_y0 = false;
@@ -1360,7 +1460,7 @@ extern "C" {
 
 int bacon_builder_new(int32_t kind, int32_t dim, bacon_builder** out) {
   if (!out) return fail(BACON_INVALID_ARGUMENT, "out is NULL");
-  if (kind < 0 || kind > 3 || dim < 1) return fail(BACON_INVALID_ARGUMENT, "bad kind or dim");
+  if (kind < 0 || kind > 6 || dim < 1) return fail(BACON_INVALID_ARGUMENT, "bad kind or dim");
   *out = new bacon_builder();
   (*out)->kind = kind;
   (*out)->dim = dim;
@@ -1377,15 +1477,25 @@ void bacon_builder_free(bacon_builder* b) { delete b; }
 
 int bacon_builder_with_tolerance(bacon_builder* b, double tol) {
   if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
+  if (b->kind == 6) return BACON_OK;  // Euler: a no-op (src/ivp.rs:390-393)
   if (tol <= 0.0) return fail(BACON_TOLERANCE_OOB, "the provided tolerance was out-of-bounds");
   b->tol = tol;
   b->has_tol = true;
   return BACON_OK;
 }
 
+// Euler keeps one step: the first value set, then the mean with each later
+// one (src/ivp.rs:395-423).
+static int euler_set_dt(bacon_builder* b, double v) {
+  b->euler_dt = b->has_euler_dt ? (b->euler_dt + v) / 2.0 : v;
+  b->has_euler_dt = true;
+  return BACON_OK;
+}
+
 int bacon_builder_with_maximum_dt(bacon_builder* b, double max) {
   if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
   if (max <= 0.0) return fail(BACON_TIME_DELTA_OOB, "the provided time delta was out-of-bounds");
+  if (b->kind == 6) return euler_set_dt(b, max);
   b->dt_max = max;
   b->has_dt_max = true;
   if (b->has_dt_min && b->dt_min > max) b->dt_min = max;
@@ -1395,6 +1505,7 @@ int bacon_builder_with_maximum_dt(bacon_builder* b, double max) {
 int bacon_builder_with_minimum_dt(bacon_builder* b, double min) {
   if (!b) return fail(BACON_INVALID_ARGUMENT, "builder is NULL");
   if (min <= 0.0) return fail(BACON_TIME_DELTA_OOB, "the provided time delta was out-of-bounds");
+  if (b->kind == 6) return euler_set_dt(b, min);
   b->dt_min = min;
   b->has_dt_min = true;
   if (b->has_dt_max && b->dt_max < min) b->dt_max = min;
@@ -1456,8 +1567,11 @@ int bacon_builder_with_derivative(bacon_builder* b, int32_t rhs, const double* p
 
 int bacon_builder_problem(const bacon_builder* b, bacon_problem* out) {
   if (!b || !out) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
-  // rk.rs:250-256 / bdf.rs:258-264: every parameter must have been set.
-  if (!b->has_dt_max || !b->has_dt_min || !b->has_tol || !b->has_t0 || !b->has_end || !b->has_y0 || b->rhs < 0)
+  // rk.rs:250-256 / bdf.rs:258-264 / adams.rs:253-259: every parameter must
+  // have been set; Euler needs no tolerance and one step size (ivp.rs:444-452).
+  const bool euler = b->kind == 6;
+  const bool have_dt = euler ? b->has_euler_dt : (b->has_dt_max && b->has_dt_min && b->has_tol);
+  if (!have_dt || !b->has_t0 || !b->has_end || !b->has_y0 || b->rhs < 0)
     return fail(BACON_MISSING_PARAMETERS, "the solver does not have all required parameters set");
   if (!b->t_ends.empty() && static_cast<int64_t>(b->t_ends.size()) != b->n)
     return fail(BACON_INVALID_ARGUMENT, "ending times and initial conditions disagree in length");
@@ -1474,9 +1588,9 @@ int bacon_builder_problem(const bacon_builder* b, bacon_problem* out) {
   out->t0_scalar = b->t0;
   out->t_end_scalar = b->t_ends.empty() ? b->t_end : 0.0;
   if (!b->t_ends.empty()) out->t_end_scalar = b->t0 + 1.0;  // unused: per-system ends given
-  out->tol = b->tol;
-  out->dt_min = b->dt_min;
-  out->dt_max = b->dt_max;
+  out->tol = euler ? 1.0 : b->tol;
+  out->dt_min = euler ? b->euler_dt : b->dt_min;
+  out->dt_max = euler ? b->euler_dt : b->dt_max;
   return BACON_OK;
 }
 

@@ -91,4 +91,93 @@ __device__ __forceinline__ double qrt(double x) {
   return __dmul_rn(r, s);
 }
 
+// One ulp-step correction of r ~ (z + adj)^(1/N), z in [1, 2^N), r in [1, 2):
+// the residual z + adj - r^N in double-double against N r^(N-1) times half an
+// ulp (the first-order distance to the rounding midpoints).
+template <int N>
+__device__ __forceinline__ double rootn_fix(double z, double r, double adj) {
+  const double r2 = __dmul_rn(r, r);
+  const double r2lo = __fma_rn(r, r, -r2);
+  double hi, lo, deriv;
+  if constexpr (N == 3) {
+    hi = __dmul_rn(r2, r);
+    lo = __fma_rn(r2lo, r, __fma_rn(r2, r, -hi));
+    deriv = __dmul_rn(3.0, r2);
+  } else {
+    const double r4 = __dmul_rn(r2, r2);
+    const double r4lo = __fma_rn(__dmul_rn(2.0, r2), r2lo, __fma_rn(r2, r2, -r4));
+    hi = __dmul_rn(r4, r);
+    lo = __fma_rn(r4lo, r, __fma_rn(r4, r, -hi));
+    deriv = __dmul_rn(5.0, r4);
+  }
+  const double res = __dadd_rn(__dsub_rn(__dsub_rn(z, hi), lo), adj);
+  const unsigned long long rb = static_cast<unsigned long long>(__double_as_longlong(r));
+  const unsigned long long e = (rb >> 52) & 0x7ffull;
+  const double half_ulp = __longlong_as_double(static_cast<long long>((e - 53ull) << 52));
+  const double thr_up = __dmul_rn(half_ulp, deriv);
+  const double thr_dn = ((rb & 0x000fffffffffffffull) == 0ull) ? __dmul_rn(0.5, thr_up) : thr_up;
+  if (res > thr_up) return __longlong_as_double(static_cast<long long>(rb + 1ull));
+  if (res < -thr_dn) return __longlong_as_double(static_cast<long long>(rb - 1ull));
+  return r;
+}
+
+// x^RN(1/N) for N = 3 or 5: what the reference's Adams controller evaluates,
+// (tol / (2 err)).powf(N.recip()) (src/ivp/adams.rs:527-528, :551-552).  The
+// rounded exponent is 1/N + delta (delta = +2^-54/5, -2^-54/3), so the value
+// is the true root times 1 + delta ln x.  Exponent split x = 2^(Nq) z with z
+// in [1, 2^N), a log-linear first guess from the bit pattern, five Newton
+// steps and an ulp-step correction give the true root; ln x (exponent plus a
+// short atanh series, relative error < 1e-5) moves it by the factor
+// 1 + delta ln x, and a second ulp-step correction on the residual of the
+// radicand z (1 + N delta ln x) rounds it.  The same operation sequence as
+// the CPU oracle's oracle_rootn; correctly rounded except within ~2^-50 ulp
+// of a midpoint.  0 -> 0, inf -> inf, negative or NaN -> NaN (as pow).
+template <int N>
+__device__ __forceinline__ double rootn(double x) {
+  static_assert(N == 3 || N == 5, "orders 3 and 5");
+  if (!(x > 0.0)) return (x == 0.0) ? 0.0 : __longlong_as_double(0x7ff8000000000000ll);
+  if (__double2hiint(x) == 0x7ff00000 && __double2loint(x) == 0) return x;  // +inf
+  double s = 1.0;
+  int shift = 0;
+  if (x < 0x1p-1000) {
+    x = __dmul_rn(x, N == 3 ? 0x1p900 : 0x1p1000);
+    s = (N == 3) ? 0x1p-300 : 0x1p-200;
+    shift = (N == 3) ? 900 : 1000;
+  }
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int e = static_cast<int>(b >> 52) - 1023;
+  int q = e / N, rem = e % N;
+  if (rem < 0) {
+    rem += N;
+    q -= 1;
+  }
+  const double z = __longlong_as_double(
+      static_cast<long long>((b & 0x000fffffffffffffull) | (static_cast<unsigned long long>(1023 + rem) << 52)));
+  double y = __longlong_as_double(static_cast<long long>(
+      0x3ff0000000000000ull +
+      (static_cast<unsigned long long>(__double_as_longlong(z)) - 0x3ff0000000000000ull) / N));
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
+    double ym1 = y;
+#pragma unroll
+    for (int k = 2; k < N; ++k) ym1 = __dmul_rn(ym1, y);
+    const double yn = __dmul_rn(ym1, y);
+    y = __dsub_rn(y, __ddiv_rn(__dsub_rn(yn, z), __dmul_rn(static_cast<double>(N), ym1)));
+  }
+  y = rootn_fix<N>(z, y, 0.0);
+  const double m = __longlong_as_double(
+      static_cast<long long>((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull));
+  const double u = __ddiv_rn(__dsub_rn(m, 1.0), __dadd_rn(m, 1.0));
+  const double u2 = __dmul_rn(u, u);
+  const double lnm = __dmul_rn(
+      __dmul_rn(2.0, u),
+      __dadd_rn(1.0, __dmul_rn(u2, __dadd_rn(1.0 / 3.0, __dmul_rn(u2, __dadd_rn(1.0 / 5.0, __dmul_rn(u2, 1.0 / 7.0)))))));
+  const double lnx = __dadd_rn(__dmul_rn(static_cast<double>(e - shift), 0.6931471805599453), lnm);
+  const double delta = (N == 3) ? -0x1p-54 / 3.0 : 0x1p-54 / 5.0;
+  const double c = __dmul_rn(delta, lnx);
+  y = __fma_rn(y, c, y);
+  y = rootn_fix<N>(z, y, __dmul_rn(z, __dmul_rn(static_cast<double>(N), c)));
+  return __dmul_rn(__dmul_rn(y, __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(1023 + q) << 52))), s);
+}
+
 }  // namespace bacon

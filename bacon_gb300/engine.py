@@ -425,3 +425,53 @@ def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_s
     if rout is not None:
         rs = RaggedSolution(rout["y"], rout["t"], rout["accepted"], rout["rejected"], rout["status"], int(code))
     return us, rs
+
+
+def adams_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order=5, max_attempts=0, traj_cap=0,
+                ctx: Context | None = None, block=0, blocks_per_sm=0, dyn_dim=False, out=None,
+                raise_on_error=False) -> Solution:
+    """Batched Adams5 / Adams3 predictor-corrector (src/ivp/adams.rs)."""
+    return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=tol, dt_min=dt_min, dt_max=dt_max, order=order,
+                       euler_dt=None, max_attempts=max_attempts, traj_cap=traj_cap, ctx=ctx, block=block,
+                       blocks_per_sm=blocks_per_sm, dyn_dim=dyn_dim, out=out, raise_on_error=raise_on_error)
+
+
+def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx: Context | None = None,
+                block=0, blocks_per_sm=0, out=None, raise_on_error=False) -> Solution:
+    """Batched Euler with a fixed step dt (src/ivp.rs:240-485)."""
+    return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=1.0, dt_min=dt, dt_max=dt, order=1, euler_dt=dt,
+                       max_attempts=max_steps, traj_cap=traj_cap, ctx=ctx, block=block,
+                       blocks_per_sm=blocks_per_sm, dyn_dim=False, out=out, raise_on_error=raise_on_error)
+
+
+def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler_dt, max_attempts, traj_cap, ctx,
+                block, blocks_per_sm, dyn_dim, out, raise_on_error) -> Solution:
+    ctx = ctx or default_context()
+    device = _is_device(y0)
+    if not device:
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        if params is not None:
+            params = np.ascontiguousarray(params, dtype=np.float64)
+        if not np.isscalar(t0):
+            t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        if not np.isscalar(t_end):
+            t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim)
+    o = _capi.AdamsOptions()
+    o.order = 5 if order == 1 else int(order)
+    o.memory = MEM_DEVICE if device else MEM_HOST
+    o.max_attempts, o.block, o.blocks_per_sm = int(max_attempts), int(block), int(blocks_per_sm)
+    if out is None:
+        out = alloc_outputs(dim, n, device, traj_cap)
+    res = make_result(out, traj_cap)
+    L = _capi.load()
+    if euler_dt is None:
+        code = L.bacon_adams_solve(ctx.handle, ctypes.byref(prob), ctypes.byref(o), ctypes.byref(res))
+    else:
+        code = L.bacon_euler_solve(ctx.handle, ctypes.byref(prob), float(euler_dt), ctypes.byref(o),
+                                   ctypes.byref(res))
+    if code in (14, 15, 16) or (raise_on_error and code != 0):
+        raise IVPError(code, _capi.last_error())
+    return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code),
+                    out.get("traj_t"), out.get("traj_y"))

@@ -29,7 +29,8 @@ from . import _capi
 from .engine import (AS_COMPILED, AS_WRITTEN, FEHLBERG, FP32_COMP, FP64_EXACT, FP64_FMA, RK23, RK45,
                      Context, IVPError, Solution, check, rk_solve)
 
-__all__ = ["Rhs", "RungeKutta45", "RungeKutta23", "BDF6", "BDF2", "IVPError", "IVPIterator", "AS_COMPILED",
+__all__ = ["Rhs", "RungeKutta45", "RungeKutta23", "BDF6", "BDF2", "Adams5", "Adams3", "Euler", "IVPError",
+           "IVPIterator", "AS_COMPILED",
            "AS_WRITTEN", "FEHLBERG", "FP64_EXACT", "FP64_FMA", "FP32_COMP"]
 
 
@@ -281,3 +282,65 @@ class RungeKutta23(_RkBuilder):
     """Bogacki-Shampine 3(2) (src/ivp/rk.rs:563-656)."""
     KIND = 1
     METHOD = RK23
+
+
+class _AdamsBuilder(_RkBuilder):
+    """Adams predictor-corrector builder (src/ivp/adams.rs:134-334): the same
+    trait methods and validation as the Runge-Kutta builders; ``solve`` runs
+    the batched Adams kernel."""
+    ORDER = 5
+
+    def _problem(self):
+        prob = _capi.Problem()
+        check(self._lib.bacon_builder_problem(self._h, ctypes.byref(prob)))
+        n, dim = int(prob.n), int(prob.dim)
+        y0 = np.ctypeslib.as_array(ctypes.cast(prob.y0, _capi.DP), shape=(dim, n)).copy()
+        params = None
+        if prob.n_params:
+            params = np.ctypeslib.as_array(ctypes.cast(prob.params, _capi.DP), shape=(prob.n_params, n)).copy()
+        t_end = prob.t_end_scalar
+        if prob.t_end:
+            t_end = np.ctypeslib.as_array(ctypes.cast(prob.t_end, _capi.DP), shape=(n,)).copy()
+        return prob, n, dim, y0, params, t_end
+
+    def _run(self, prob, y0, params, t_end, cap, ctx, max_attempts):
+        from .engine import adams_solve
+        return adams_solve(y0, params, prob.t0_scalar, t_end, rhs=prob.rhs, tol=prob.tol, dt_min=prob.dt_min,
+                           dt_max=prob.dt_max, order=self.ORDER, max_attempts=max_attempts, traj_cap=cap, ctx=ctx,
+                           dyn_dim=bool(prob.dyn_dim))
+
+    def solve(self, data=None, *, max_attempts: int = 0, record_path: bool | None = None,
+              path_capacity: int = 4096, ctx: Context | None = None, **_ignored) -> IVPIterator:
+        prob, n, dim, y0, params, t_end = self._problem()
+        if record_path is None:
+            record_path = n <= 64
+        cap = path_capacity if record_path else 0
+        while True:
+            sol = self._run(prob, y0, params, t_end, cap, ctx, max_attempts)
+            if not cap or int(np.max(sol.accepted)) <= cap:
+                break
+            cap = int(np.max(sol.accepted)) + 1
+        return IVPIterator(sol, n, dim)
+
+
+class Adams5(_AdamsBuilder):
+    """5th-order Adams predictor-corrector (src/ivp/adams.rs:605-634)."""
+    KIND = 4
+    ORDER = 5
+
+
+class Adams3(_AdamsBuilder):
+    """3rd-order Adams predictor-corrector (src/ivp/adams.rs:661-694)."""
+    KIND = 5
+    ORDER = 3
+
+
+class Euler(_AdamsBuilder):
+    """Euler's method (src/ivp.rs:240-485): with_tolerance is a no-op and the
+    step is the first dt given, then the mean with each later one."""
+    KIND = 6
+
+    def _run(self, prob, y0, params, t_end, cap, ctx, max_attempts):
+        from .engine import euler_solve
+        return euler_solve(y0, params, prob.t0_scalar, t_end, rhs=prob.rhs, dt=prob.dt_max,
+                           max_steps=max_attempts, traj_cap=cap, ctx=ctx)

@@ -233,6 +233,34 @@ typedef struct {
 int bacon_bdf_solve(bacon_ctx* ctx, const bacon_problem* problem,
                     const bacon_bdf_options* options, bacon_rk_result* result);
 
+/* ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) -- */
+typedef struct {
+  int32_t order;          /* 5 (Adams5) or 3 (Adams3); ignored by Euler */
+  int32_t memory;         /* bacon_memory */
+  int64_t max_attempts;   /* cap on step() calls per system, 0 = 10,000,000 */
+  int32_t block;          /* 0 = 128 */
+  int32_t blocks_per_sm;  /* 0 = occupancy model */
+} bacon_adams_options;
+
+/* Batched Adams5 / Adams3 (AdamsSolver::step, src/ivp/adams.rs:411-565, with
+ * its RK4 bootstrap :344-395 and the iterator of src/ivp.rs:214-238), one
+ * system per thread.  dt0 = (dt_max + dt_min) / 2 (adams.rs:310).  The step
+ * factor (tol / (2 err))^(1/O) is x^RN(1/O) evaluated by a fixed IEEE
+ * operation sequence (correctly rounded except within ~2^-50 ulp of a
+ * midpoint).  Same result semantics as bacon_rk_solve: the last yielded item,
+ * accepted = items yielded, rejected = Redo count.  RHS: EXP/DECAY (dim 1,
+ * 2), QUADRATIC, SINE (dim 1), HARMONIC, VDP, LORENZ, LOTKA. */
+int bacon_adams_solve(bacon_ctx* ctx, const bacon_problem* problem,
+                      const bacon_adams_options* options, bacon_rk_result* result);
+
+/* Batched Euler (EulerSolver::step, src/ivp.rs:318-339) with the builder's
+ * step dt (with_maximum_dt / with_minimum_dt: the first value set, then the
+ * mean with each later one, src/ivp.rs:395-423).  The iterator yields the
+ * state each step starts from, so the last yielded item is the state at the
+ * start of the final step.  problem->tol, dt_min and dt_max are unused. */
+int bacon_euler_solve(bacon_ctx* ctx, const bacon_problem* problem, double dt,
+                      const bacon_adams_options* options, bacon_rk_result* result);
+
 /* A batch of systems of one right-hand side whose sizes differ.  System i's
  * state is y0[y_offsets[i] .. y_offsets[i+1]) and its parameters
  * params[p_offsets[i] .. p_offsets[i+1]).  In the reference each is its own
@@ -339,9 +367,13 @@ int bacon_rk_validate(const bacon_problem* problem);
 /* ---- builder (mirrors the IVPSolver trait, src/ivp.rs:134-190) ---------- */
 typedef struct bacon_builder bacon_builder;
 
-/* kind: 0 = RungeKutta45, 1 = RungeKutta23, 2 = BDF6, 3 = BDF2.
- * bacon_builder_new mirrors IVPSolver::new (static dimension `dim`);
- * bacon_builder_new_dyn mirrors new_dyn(size). */
+/* kind: 0 = RungeKutta45, 1 = RungeKutta23, 2 = BDF6, 3 = BDF2, 4 = Adams5,
+ * 5 = Adams3, 6 = Euler.  bacon_builder_new mirrors IVPSolver::new (static
+ * dimension `dim`); bacon_builder_new_dyn mirrors new_dyn(size).  For Euler,
+ * with_tolerance is a no-op and with_maximum_dt / with_minimum_dt set one
+ * step size (the first value, then the mean with each later one,
+ * src/ivp.rs:389-423); bacon_builder_problem then puts that step in dt_min
+ * and dt_max. */
 int bacon_builder_new(int32_t kind, int32_t dim, bacon_builder** out);
 int bacon_builder_new_dyn(int32_t kind, int32_t size, bacon_builder** out);
 void bacon_builder_free(bacon_builder* b);

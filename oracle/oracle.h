@@ -150,6 +150,31 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
                              double* t_out, int64_t* accepted, int64_t* rejected,
                              double* traj_t, double* traj_y, int64_t traj_cap);
 
+/* ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) -- */
+typedef struct {
+  int32_t order;         /* 5 (Adams5) or 3 (Adams3) */
+  int32_t pow_mode;      /* ORC_POW_QRT: oracle_rootn; ORC_POW_LIBM: pow */
+  int32_t dyn_dim;       /* 1: nalgebra Dyn vector (norm summation order) */
+  int32_t reserved;
+  int64_t max_attempts;  /* extension: cap on step() calls, 0 = none */
+  double tol, dt_min, dt_max;
+} oracle_adams_cfg;
+
+/* x^(1/n), n = 3 or 5, as a fixed sequence of IEEE operations. */
+double oracle_rootn(double x, int n);
+
+int32_t oracle_adams_solve_one(const oracle_adams_cfg* cfg, int32_t rhs, int32_t dim,
+                               const double* p, const double* shared, double t0,
+                               double t_end, const double* y0, double* y_out,
+                               double* t_out, int64_t* accepted, int64_t* rejected,
+                               double* traj_t, double* traj_y, int64_t traj_cap);
+
+int32_t oracle_euler_solve_one(int32_t rhs, int32_t dim, const double* p, const double* shared,
+                               double dt, int64_t max_steps, double t0, double t_end,
+                               const double* y0, double* y_out, double* t_out,
+                               int64_t* accepted, double* traj_t, double* traj_y,
+                               int64_t traj_cap);
+
 /* ---- gradients (no reference counterpart; oracle for the adjoint) ------- */
 /* Discrete adjoint of the accepted-step sequence of a forward solve (step
  * sizes frozen), loss = sum_d (y_T[d] - target[d])^2.  Fills dL/dy0[dim] and

@@ -39,6 +39,19 @@ class _RkCfg(ctypes.Structure):
     ]
 
 
+class _AdamsCfg(ctypes.Structure):
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("pow_mode", ctypes.c_int32),
+        ("dyn_dim", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("max_attempts", ctypes.c_int64),
+        ("tol", ctypes.c_double),
+        ("dt_min", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+    ]
+
+
 class _BdfCfg(ctypes.Structure):
     _fields_ = [
         ("method", ctypes.c_int32),
@@ -93,6 +106,17 @@ def lib():
             L.oracle_bdf_solve_one.argtypes = [
                 ctypes.POINTER(_BdfCfg), ctypes.c_int32, ctypes.c_int32, dp, dp,
                 ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
+        if hasattr(L, "oracle_adams_solve_one"):
+            L.oracle_rootn.restype = ctypes.c_double
+            L.oracle_rootn.argtypes = [ctypes.c_double, ctypes.c_int]
+            L.oracle_adams_solve_one.restype = ctypes.c_int32
+            L.oracle_adams_solve_one.argtypes = [
+                ctypes.POINTER(_AdamsCfg), ctypes.c_int32, ctypes.c_int32, dp, dp,
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
+            L.oracle_euler_solve_one.restype = ctypes.c_int32
+            L.oracle_euler_solve_one.argtypes = [
+                ctypes.c_int32, ctypes.c_int32, dp, dp, ctypes.c_double, ctypes.c_int64,
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, dp, dp, ctypes.c_int64]
         if hasattr(L, "oracle_rk_adjoint_one"):
             L.oracle_rk_adjoint_one.restype = ctypes.c_int32
             L.oracle_rk_adjoint_one.argtypes = [
@@ -265,3 +289,55 @@ def bdf_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0)
         n = min(a.value, traj_cap)
         tt, ty = tt[:n], ty[:n]
     return Path(st, t.value, y, a.value, r.value, tt, ty)
+
+
+# ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) ----
+def adams_cfg(order=5, pow_mode=POW_QRT, dyn_dim=False, max_attempts=0, tol=1e-6, dt_min=1e-6, dt_max=0.1):
+    return _AdamsCfg(int(order), int(pow_mode), int(dyn_dim), 0, int(max_attempts), tol, dt_min, dt_max)
+
+
+def rootn(x: float, n: int) -> float:
+    return lib().oracle_rootn(float(x), int(n))
+
+
+def adams_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0) -> Path:
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    dim = y0.shape[0]
+    p = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    y = np.zeros(dim)
+    t = ctypes.c_double()
+    a = ctypes.c_int64()
+    r = ctypes.c_int64()
+    tt = ty = None
+    if traj_cap:
+        tt = np.zeros(traj_cap)
+        ty = np.zeros((traj_cap, dim))
+    st = L.oracle_adams_solve_one(ctypes.byref(cfg), rhs, dim, _dp(p), _dp(sh), t0, t_end, _dp(y0), _dp(y),
+                                  ctypes.byref(t), ctypes.byref(a), ctypes.byref(r), _dp(tt), _dp(ty), traj_cap)
+    if traj_cap:
+        n = min(a.value, traj_cap)
+        tt, ty = tt[:n], ty[:n]
+    return Path(st, t.value, y, a.value, r.value, tt, ty)
+
+
+def euler_solve_one(rhs, y0, t0, t_end, dt, params=None, shared=None, max_steps=0, traj_cap=0) -> Path:
+    L = lib()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    dim = y0.shape[0]
+    p = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float64)
+    sh = None if shared is None else np.ascontiguousarray(shared, dtype=np.float64)
+    y = np.zeros(dim)
+    t = ctypes.c_double()
+    a = ctypes.c_int64()
+    tt = ty = None
+    if traj_cap:
+        tt = np.zeros(traj_cap)
+        ty = np.zeros((traj_cap, dim))
+    st = L.oracle_euler_solve_one(rhs, dim, _dp(p), _dp(sh), dt, int(max_steps), t0, t_end, _dp(y0), _dp(y),
+                                  ctypes.byref(t), ctypes.byref(a), _dp(tt), _dp(ty), traj_cap)
+    if traj_cap:
+        n = min(a.value, traj_cap)
+        tt, ty = tt[:n], ty[:n]
+    return Path(st, t.value, y, a.value, 0, tt, ty)
