@@ -188,6 +188,12 @@ def other_cpu_baselines(W):
                                                  lv.extra["target"][:, i]), idx, threads)
     out["adjoint"] = {"value": len(idx) / sec, "unit": "grads/s", "cores": threads,
                       "sample": f"{len(idx)} of the 262144 Lotka-Volterra systems"}
+    sub = vb.subset(np.arange(0, vb.n, vb.n // (8 * threads)))
+    acfg = O.adams_cfg(order=5, tol=sub.tol, dt_min=sub.dt_min, dt_max=sub.dt_max)
+    _, sec = cpu_pool(lambda i: O.adams_solve_one(acfg, sub.rhs, sub.y0[:, i], 0.0, 10.0, params=sub.params[:, i]),
+                      range(sub.n), threads)
+    out["adams5_van_der_pol_4096"] = {"value": sub.n / sec, "unit": "solves/s", "cores": threads,
+                                      "sample": f"{sub.n} of the 4096 Van der Pol systems"}
     rob, ch = W.stiff_batch(131072)
     k = 4 * threads
     ri = np.linspace(0, rob.n - 1, k).astype(int)
@@ -224,6 +230,19 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
     ms = ctx.last_kernel_ms()
     out["van_der_pol_4096"] = {"value": vb.n / (ms * 1e-3), "unit": "solves/s", "kernel_ms": ms,
                                "statuses_ok": bool((s.status == 0).all().item())}
+
+    # The same Van der Pol batch with Adams5 (the reference's predictor-
+    # corrector, src/ivp/adams.rs): it restarts from an RK4 bootstrap after
+    # every dt change, so it takes ~10^5 step calls per system.
+    E.adams_solve(vy, vp, 0.0, 10.0, rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5, ctx=ctx)
+    a5 = E.adams_solve(vy, vp, 0.0, 10.0, rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5,
+                       ctx=ctx)
+    ams = ctx.last_kernel_ms()
+    st = a5.status.cpu().numpy()
+    out["adams5_van_der_pol_4096"] = {
+        "value": vb.n / (ams * 1e-3), "unit": "solves/s", "kernel_ms": ams,
+        "status_counts": {int(k): int((st == k).sum()) for k in np.unique(st)},
+        "step_calls_mean": float((a5.accepted.double() + a5.rejected.double()).mean().item())}
 
     # Linear y' = A y, shared A (n = 256), 65,536 states, tol 1e-8.
     lb = W.linear_shared()

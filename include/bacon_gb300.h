@@ -8,6 +8,8 @@
  *   RungeKuttaSolver::step             src/ivp/rk.rs:361-423
  *   IVPIterator::next / collect_vec    src/ivp.rs:192-239
  *   BDF builder / BDFSolver::step      src/ivp/bdf.rs:124-332, :495-634
+ *   Adams builder / AdamsSolver::step  src/ivp/adams.rs:134-334, :344-565
+ *   Euler builder / EulerSolver::step  src/ivp.rs:240-485
  *   IVPError                           src/ivp.rs:50-76
  *
  * All entry points are plain C: pointers, sizes and status codes.  Every
