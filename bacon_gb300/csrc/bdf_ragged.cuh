@@ -9,11 +9,11 @@
 // conflict-free read across the group), the pivot reciprocals and the row
 // permutation, the history H[0..6], the interpolated history HH, a staging
 // vector, the parameters and a small exchange area for broadcasts and
-// reductions.  The substitutions are a dependent chain over the pivots: the
-// owner of row i publishes x_i (a shuffle within one warp, else a shared-
-// memory slot and the group's named barrier) and every other row updates
-// itself, so a large system keeps G warps issuing instead of one warp running
-// G rows per lane.
+// reductions.  The substitutions go by 32-row blocks: the block's warp runs
+// its triangle with shuffles (the dependent chain over the pivots stays
+// inside one warp), publishes the 32 values through shared memory and the
+// group's named barrier, and the other warps apply them to their rows while
+// the next block's warp already works on its own triangle.
 //
 // Factors are costly to recompute (2/3 dim^3 flops) and the chain Jacobian is
 // constant, so M depends on h b_q alone.  A solve meets ~100 distinct values
@@ -67,8 +67,9 @@ __host__ __device__ constexpr int rag_class_of(int dim) { return dim > 96 ? 0 : 
 // One group's shared-memory slice for systems of dim <= ld, in doubles:
 // factors ld*ld, pivot reciprocals ld, H 7*ld, HH 7*ld, staging ld, params
 // ld/2+2, permutation ld/2 (ld ints), cache table 48 (16 keys, 16 stamps,
-// 16 states), exchange area 16 (2 broadcast slots, 2 x 4 reduction values,
-// 2 x 4 reduction indices).
+// 16 states), exchange area 80 (2 broadcast slots, 2 x 4 reduction values,
+// 2 x 4 reduction indices, the work item, 2 x 32 block values of the
+// substitutions).
 struct RagSmem {
   __host__ __device__ static constexpr int M(int) { return 0; }
   __host__ __device__ static constexpr int rinv(int ld) { return ld * ld; }
@@ -79,7 +80,7 @@ struct RagSmem {
   __host__ __device__ static constexpr int perm(int ld) { return ld * ld + 16 * ld + ld / 2 + 2; }
   __host__ __device__ static constexpr int table(int ld) { return perm(ld) + ld / 2; }
   __host__ __device__ static constexpr int xch(int ld) { return table(ld) + 48; }
-  __host__ __device__ static constexpr int doubles(int ld) { return xch(ld) + 16; }
+  __host__ __device__ static constexpr int doubles(int ld) { return xch(ld) + 80; }
 };
 
 // Shared memory of a CTA for the classes present (bit c of mask = class c).
@@ -400,16 +401,48 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
     if (own) sv[r] = gr;
     g.sync();
     double dx = own ? -sv[src] : 0.0;
-    // forward substitution with the unit lower factor
-    for (int i = 0; i + 1 < D; ++i) {
-      const double xi = g.bcast(dx, i, i);
-      if (r > i && own) dx = O::sub(dx, O::mul(M[i * D + r], xi));
+    // Substitutions by 32-row blocks (block b = warp b of the group): the
+    // block's warp runs its triangle with shuffles, publishes the 32 values
+    // once, and the other warps apply them to their rows in pivot order, so
+    // every row receives its updates in the order of the unblocked loops.
+    const int wg = r >> 5, lane = r & 31;
+    const int nblk = (D + 31) >> 5;
+    double* xs = g.xch + 16;  // [2][32], alternating blocks
+    // forward, unit lower factor
+    for (int b = 0; b < nblk; ++b) {
+      const int base = 32 * b;
+      const int nb = min(32, D - base);
+      if (wg == b) {
+        for (int ii = 0; ii + 1 < nb; ++ii) {
+          const double xi = __shfl_sync(0xffffffffu, dx, ii);
+          if (lane > ii && own) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xi));
+        }
+        if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
+      }
+      if (nblk > 1) {
+        g.sync();
+        if (wg > b && own)
+          for (int ii = 0; ii < nb; ++ii) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xs[(b & 1) * 32 + ii]));
+      }
     }
-    // back substitution with the upper factor
-    for (int i = D - 1; i >= 0; --i) {
-      if (r == i) dx = O::mul(dx, srinv[i]);
-      const double xi = g.bcast(dx, i, i);
-      if (r < i) dx = O::sub(dx, O::mul(M[i * D + r], xi));
+    // back, upper factor (multiplying by the elimination's pivot reciprocals)
+    for (int b = nblk - 1; b >= 0; --b) {
+      const int base = 32 * b;
+      const int nb = min(32, D - base);
+      if (wg == b) {
+        for (int ii = nb - 1; ii >= 0; --ii) {
+          if (lane == ii) dx = O::mul(dx, srinv[base + ii]);
+          const double xi = __shfl_sync(0xffffffffu, dx, ii);
+          if (lane < ii) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xi));
+        }
+        if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
+      }
+      if (nblk > 1) {
+        g.sync();
+        if (wg < b)
+          for (int ii = nb - 1; ii >= 0; --ii)
+            dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xs[(b & 1) * 32 + ii]));
+      }
     }
     if (own) {
       y = O::add(y, dx);
