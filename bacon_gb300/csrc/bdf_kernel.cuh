@@ -10,7 +10,9 @@
 // double dt below tol/10 (here only with a full history, re-sampling every
 // second point), halve on rejection (Lagrange re-interpolation of the
 // history), MinimumTimeDeltaExceeded below dt_min.  The operation sequence is
-// the CPU oracle's (oracle/bdf_oracle.c, bdf_corrected), in exact FP64.
+// the CPU oracle's (oracle/bdf_oracle.c, bdf_corrected), in exact FP64; the
+// LU elimination and both substitutions update with fused multiply-adds
+// (correctly rounded, so the oracle's C fma gives the same bits).
 #pragma once
 
 #include "rk_kernel.cuh"
@@ -168,7 +170,7 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
       const double l = O::mul(M[r][i], inv);
       M[r][i] = l;
 #pragma unroll
-      for (int k = i + 1; k < D; ++k) M[r][k] = O::sub(M[r][k], O::mul(l, M[i][k]));
+      for (int k = i + 1; k < D; ++k) M[r][k] = __fma_rn(-l, M[i][k], M[r][k]);
     }
   }
   const double conv = O::mul(1e-3, tol);
@@ -193,12 +195,12 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
 #pragma unroll
     for (int i = 0; i < D; ++i)
 #pragma unroll
-      for (int r = i + 1; r < D; ++r) dx[r] = O::sub(dx[r], O::mul(M[r][i], dx[i]));
+      for (int r = i + 1; r < D; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
 #pragma unroll
     for (int i = D - 1; i >= 0; --i) {
       dx[i] = O::mul(dx[i], rinv[i]);
 #pragma unroll
-      for (int r = 0; r < i; ++r) dx[r] = O::sub(dx[r], O::mul(M[r][i], dx[i]));
+      for (int r = 0; r < i; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
     }
     double dn = 0.0;
 #pragma unroll

@@ -36,8 +36,8 @@
 // operands in the same order, so the results are bit-identical to them:
 //   - partial-pivot LU: pivot = first row of maximum |M[r][i]| (a group
 //     arg-max with lowest-index ties), whole-row swaps, l = M[r][i] * (1 /
-//     M[i][i]), M[r][k] -= l M[i][k] row by row and pivot by pivot;
-//   - substitutions: row r receives its updates in pivot order, the back
+//     M[i][i]), M[r][k] = fma(-l, M[i][k], M[r][k]) pivot by pivot;
+//   - substitutions: row r receives its fused updates in pivot order, the back
 //     substitution multiplies by the pivot reciprocals the elimination
 //     formed; the permutation is applied as one gather (it only moves
 //     values);
@@ -282,7 +282,7 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
       col[r] = l;
       for (int k = i + 1; k < D; ++k) {
         double* ck = M + k * D;
-        ck[r] = O::sub(ck[r], O::mul(l, ck[i]));
+        ck[r] = __fma_rn(-l, ck[i], ck[r]);
       }
     }
     g.sync();
@@ -415,14 +415,14 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
       if (wg == b) {
         for (int ii = 0; ii + 1 < nb; ++ii) {
           const double xi = __shfl_sync(0xffffffffu, dx, ii);
-          if (lane > ii && own) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xi));
+          if (lane > ii && own) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
         }
         if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
       }
       if (nblk > 1) {
         g.sync();
         if (wg > b && own)
-          for (int ii = 0; ii < nb; ++ii) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xs[(b & 1) * 32 + ii]));
+          for (int ii = 0; ii < nb; ++ii) dx = __fma_rn(-M[(base + ii) * D + r], xs[(b & 1) * 32 + ii], dx);
       }
     }
     // back, upper factor (multiplying by the elimination's pivot reciprocals)
@@ -433,7 +433,7 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
         for (int ii = nb - 1; ii >= 0; --ii) {
           if (lane == ii) dx = O::mul(dx, srinv[base + ii]);
           const double xi = __shfl_sync(0xffffffffu, dx, ii);
-          if (lane < ii) dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xi));
+          if (lane < ii) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
         }
         if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
       }
@@ -441,7 +441,7 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
         g.sync();
         if (wg < b)
           for (int ii = nb - 1; ii >= 0; --ii)
-            dx = O::sub(dx, O::mul(M[(base + ii) * D + r], xs[(b & 1) * 32 + ii]));
+            dx = __fma_rn(-M[(base + ii) * D + r], xs[(b & 1) * 32 + ii], dx);
       }
     }
     if (own) {
