@@ -173,6 +173,11 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
       for (int k = i + 1; k < D; ++k) M[r][k] = __fma_rn(-l, M[i][k], M[r][k]);
     }
   }
+  // rows of U scaled by their pivot reciprocal (a unit upper factor)
+#pragma unroll
+  for (int r = 0; r < D; ++r)
+#pragma unroll
+    for (int k = r + 1; k < D; ++k) M[r][k] = O::mul(M[r][k], rinv[r]);
   const double conv = O::mul(1e-3, tol);
   for (int it = 0; it < max_newton; ++it) {
     double f[D], dx[D];
@@ -197,11 +202,11 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
 #pragma unroll
       for (int r = i + 1; r < D; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
 #pragma unroll
-    for (int i = D - 1; i >= 0; --i) {
-      dx[i] = O::mul(dx[i], rinv[i]);
+    for (int r = 0; r < D; ++r) dx[r] = O::mul(dx[r], rinv[r]);
+#pragma unroll
+    for (int i = D - 1; i > 0; --i)
 #pragma unroll
       for (int r = 0; r < i; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
-    }
     double dn = 0.0;
 #pragma unroll
     for (int d = 0; d < D; ++d) {

@@ -11,9 +11,10 @@
 // vector, the parameters and a small exchange area for broadcasts and
 // reductions.  The substitutions go by 32-row blocks: the block's warp runs
 // its triangle with shuffles (the dependent chain over the pivots stays
-// inside one warp), publishes the 32 values through shared memory and the
-// group's named barrier, and the other warps apply them to their rows while
-// the next block's warp already works on its own triangle.
+// inside one warp) and publishes the values in chunks of 8 or 16 through
+// shared memory, arriving on a named barrier per chunk without waiting; the
+// warps below wait on it and apply each chunk while the block's warp
+// continues, so the next block's warp starts its triangle almost at once.
 //
 // Factors are costly to recompute (2/3 dim^3 flops) and the chain Jacobian is
 // constant, so M depends on h b_q alone.  A solve meets ~100 distinct values
@@ -37,10 +38,12 @@
 //   - partial-pivot LU: pivot = first row of maximum |M[r][i]| (a group
 //     arg-max with lowest-index ties), whole-row swaps, l = M[r][i] * (1 /
 //     M[i][i]), M[r][k] = fma(-l, M[i][k], M[r][k]) pivot by pivot;
-//   - substitutions: row r receives its fused updates in pivot order, the back
-//     substitution multiplies by the pivot reciprocals the elimination
-//     formed; the permutation is applied as one gather (it only moves
-//     values);
+//   - the rows of U are then scaled by the pivot reciprocals the elimination
+//     formed (a unit upper factor, so no product sits on the back
+//     substitution's chain); the back substitution scales its right-hand
+//     side by them once;
+//   - substitutions: row r receives its fused updates in pivot order; the
+//     permutation is applied as one gather (it only moves values);
 //   - the Newton step norm and the error norm only feed comparisons with
 //     thresholds: a group tree sum decides them unless it lies within 1e-10
 //     of a threshold, where the oracle's ordered sum on one thread decides.
@@ -51,6 +54,11 @@
 #include "bdf_kernel.cuh"
 
 namespace bacon {
+
+#ifndef BACON_BAR_ARRIVE
+#define BACON_BAR_ARRIVE(id, cnt) \
+  asm volatile("bar.arrive %0, %1;" ::"r"(static_cast<unsigned>(id)), "r"(static_cast<unsigned>(cnt)) : "memory")
+#endif
 
 constexpr int kRagMaxDim = 128;
 constexpr int kRagWarps = 8;  // warps per CTA
@@ -63,6 +71,10 @@ __host__ __device__ constexpr int rag_class_dim(int c) { return c == 0 ? 128 : c
 __host__ __device__ constexpr int rag_class_gwarps(int c) { return c == 0 ? 4 : c == 1 ? 3 : c == 2 ? 2 : 1; }
 __host__ __device__ constexpr int rag_class_groups(int c) { return c == 0 ? 1 : c == 1 ? 2 : c == 2 ? 4 : 8; }
 __host__ __device__ constexpr int rag_class_of(int dim) { return dim > 96 ? 0 : dim > 64 ? 1 : dim > 32 ? 2 : 3; }
+// Chunks per 32-row block in the substitutions' hand-off.  Named barrier ids:
+// 0 is __syncthreads, 1..groups the groups' own, then each group's chunk
+// barriers (at most 1 + 4 + 4*2 = 12 < 16).
+__host__ __device__ constexpr int rag_class_chunks(int c) { return c <= 1 ? 4 : c == 2 ? 2 : 0; }
 
 // One group's shared-memory slice for systems of dim <= ld, in doubles:
 // factors ld*ld, pivot reciprocals ld, H 7*ld, HH 7*ld, staging ld, params
@@ -170,8 +182,17 @@ struct RagGroup {
   int t;         // thread (= row) index in the group
   int nthr;      // 32 * warps
   int bar;       // named barrier id
+  int cbar;      // first of the substitutions' chunk barrier ids
+  int nchunk;    // chunks per 32-row block (0 for a one-warp group)
   double* xch;   // exchange area (RagSmem::xch)
   int par;       // parity of the next reduction's buffer
+
+  // Producer/consumer hand-off on a named barrier: the producing warp
+  // arrives (and moves on), the consuming warps wait.  cnt counts both.
+  __device__ __forceinline__ static void arrive(int id, unsigned cnt) { BACON_BAR_ARRIVE(id, cnt); }
+  __device__ __forceinline__ static void wait(int id, unsigned cnt) {
+    __barrier_sync_count(static_cast<unsigned>(id), cnt);
+  }
 
   __device__ __forceinline__ void sync() const {
     if (nthr == 32) __syncwarp();
@@ -287,6 +308,12 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
     }
     g.sync();
   }
+  // the rows of U scaled by their pivot reciprocal (a unit upper factor for
+  // the back substitution); the caller syncs before the factors are read
+  if (r < D) {
+    const double s = rinv[r];
+    for (int k = r + 1; k < D; ++k) M[k * D + r] = O::mul(M[k * D + r], s);
+  }
   return true;
 }
 
@@ -401,47 +428,75 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
     if (own) sv[r] = gr;
     g.sync();
     double dx = own ? -sv[src] : 0.0;
-    // Substitutions by 32-row blocks (block b = warp b of the group): the
-    // block's warp runs its triangle with shuffles, publishes the 32 values
-    // once, and the other warps apply them to their rows in pivot order, so
-    // every row receives its updates in the order of the unblocked loops.
+    // Substitutions by 32-row blocks (block b = warp b of the group).  The
+    // block's warp runs its triangle with shuffles and publishes the values
+    // chunk by chunk (it arrives on the chunk's barrier and moves on); the
+    // warps that need them wait on that barrier and apply the chunk while the
+    // block's warp continues.  Every row receives its updates in the order of
+    // the unblocked loops.  A chunk barrier is reused by the next block only
+    // after every participant of its previous phase has arrived: the next
+    // block's warps all waited on the earlier chunks.
     const int wg = r >> 5, lane = r & 31;
     const int nblk = (D + 31) >> 5;
     double* xs = g.xch + 16;  // [2][32], alternating blocks
+    const int cs = g.nchunk > 0 ? 32 / g.nchunk : 32;
     // forward, unit lower factor
     for (int b = 0; b < nblk; ++b) {
       const int base = 32 * b;
       const int nb = min(32, D - base);
+      const unsigned cnt = 32u * static_cast<unsigned>(nblk - b);
+      double* xb = xs + (b & 1) * 32;
       if (wg == b) {
-        for (int ii = 0; ii + 1 < nb; ++ii) {
-          const double xi = __shfl_sync(0xffffffffu, dx, ii);
-          if (lane > ii && own) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+        for (int lo = 0; lo < nb; lo += cs) {
+          const int hi = min(lo + cs, nb);
+          for (int ii = lo; ii < hi && ii + 1 < nb; ++ii) {
+            const double xi = __shfl_sync(0xffffffffu, dx, ii);
+            if (lane > ii && own) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+          }
+          if (b + 1 < nblk) {
+            if (lane >= lo && lane < hi) xb[lane] = dx;
+            g.arrive(g.cbar + lo / cs, cnt);
+          }
         }
-        if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
-      }
-      if (nblk > 1) {
-        g.sync();
-        if (wg > b && own)
-          for (int ii = 0; ii < nb; ++ii) dx = __fma_rn(-M[(base + ii) * D + r], xs[(b & 1) * 32 + ii], dx);
+      } else if (wg > b) {
+        for (int lo = 0; lo < nb; lo += cs) {
+          const int hi = min(lo + cs, nb);
+          g.wait(g.cbar + lo / cs, cnt);
+          if (own)
+            for (int ii = lo; ii < hi; ++ii) dx = __fma_rn(-M[(base + ii) * D + r], xb[ii], dx);
+        }
       }
     }
-    // back, upper factor (multiplying by the elimination's pivot reciprocals)
+    // back, on the row-scaled unit upper factor.  The group sync closes every
+    // forward chunk phase first: warp 0 only arrived on block 0's chunk
+    // barriers, and its waits below use the same ids.  It costs no time on
+    // the critical path (the last block's warp finishes the forward last and
+    // starts the back first).
+    if (nblk > 1) g.sync();
+    if (own) dx = O::mul(dx, srinv[r]);
     for (int b = nblk - 1; b >= 0; --b) {
       const int base = 32 * b;
       const int nb = min(32, D - base);
+      const unsigned cnt = 32u * static_cast<unsigned>(b + 1);
+      double* xb = xs + (b & 1) * 32;
       if (wg == b) {
-        for (int ii = nb - 1; ii >= 0; --ii) {
-          if (lane == ii) dx = O::mul(dx, srinv[base + ii]);
-          const double xi = __shfl_sync(0xffffffffu, dx, ii);
-          if (lane < ii) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+        for (int hi = nb; hi > 0; hi -= cs) {
+          const int lo = max(hi - cs, 0);
+          for (int ii = hi - 1; ii >= lo && ii > 0; --ii) {
+            const double xi = __shfl_sync(0xffffffffu, dx, ii);
+            if (lane < ii) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+          }
+          if (b > 0) {
+            if (lane >= lo && lane < hi) xb[lane] = dx;
+            g.arrive(g.cbar + (nb - hi) / cs, cnt);
+          }
         }
-        if (nblk > 1) xs[(b & 1) * 32 + lane] = dx;
-      }
-      if (nblk > 1) {
-        g.sync();
-        if (wg < b)
-          for (int ii = nb - 1; ii >= 0; --ii)
-            dx = __fma_rn(-M[(base + ii) * D + r], xs[(b & 1) * 32 + ii], dx);
+      } else if (wg < b) {
+        for (int hi = nb; hi > 0; hi -= cs) {
+          const int lo = max(hi - cs, 0);
+          g.wait(g.cbar + (nb - hi) / cs, cnt);
+          for (int ii = hi - 1; ii >= lo; --ii) dx = __fma_rn(-M[(base + ii) * D + r], xb[ii], dx);
+        }
       }
     }
     if (own) {
@@ -682,6 +737,8 @@ __global__ void __launch_bounds__(kRagWarps * 32, 1)
       g.t = static_cast<int>(threadIdx.x) - grp * gw * 32;
       g.nthr = gw * 32;
       g.bar = 1 + grp;
+      g.nchunk = rag_class_chunks(c);
+      g.cbar = 1 + rag_class_groups(c) + grp * g.nchunk;
       g.xch = ws + RagSmem::xch(ld);
       g.par = 0;
       double* gcache = gcache_cta + static_cast<size_t>(grp) * rag_gcache_group_doubles(c);

@@ -424,6 +424,10 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
       for (int k = i + 1; k < n; ++k) M[r][k] = fma(-l, M[i][k], M[r][k]);
     }
   }
+  /* the rows of U scaled by their pivot reciprocal: the back substitution
+   * then runs on a unit upper factor, with no product on its critical path */
+  for (int r = 0; r < n; ++r)
+    for (int k = r + 1; k < n; ++k) M[r][k] = M[r][k] * rinv[r];
   const int max_newton = cfg->max_iter > 0 ? cfg->max_iter : 8;
   for (int it = 0; it < max_newton; ++it) {
     oracle_rhs(rhs, n, t1, y, p, shared, f);
@@ -434,12 +438,11 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
       if (piv[i] != i) { const double t = dx[i]; dx[i] = dx[piv[i]]; dx[piv[i]] = t; }
     for (int i = 0; i < n; ++i)
       for (int r = i + 1; r < n; ++r) dx[r] = fma(-M[r][i], dx[i], dx[r]);
-    /* back substitution multiplies by the reciprocal the elimination formed
-     * (no division on the solve's critical path) */
-    for (int i = n - 1; i >= 0; --i) {
-      dx[i] = dx[i] * rinv[i];
+    /* back substitution on the row-scaled upper factor: the right-hand side
+     * takes the pivot reciprocals first (the elimination's own, no division) */
+    for (int r = 0; r < n; ++r) dx[r] = dx[r] * rinv[r];
+    for (int i = n - 1; i > 0; --i)
       for (int r = 0; r < i; ++r) dx[r] = fma(-M[r][i], dx[i], dx[r]);
-    }
     double dn = 0.0;
     for (int d = 0; d < n; ++d) {
       y[d] = y[d] + dx[d];
