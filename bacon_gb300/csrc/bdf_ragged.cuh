@@ -60,6 +60,58 @@ namespace bacon {
   asm volatile("bar.arrive %0, %1;" ::"r"(static_cast<unsigned>(id)), "r"(static_cast<unsigned>(cnt)) : "memory")
 #endif
 
+// Bulk copies into shared memory through the async proxy, tracked on an
+// mbarrier.  (A host build of this header for testing supplies its own
+// versions by defining BACON_RAG_HOST_SHIMS.)
+#ifndef BACON_RAG_HOST_SHIMS
+__device__ __forceinline__ uint32_t rag_smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void rag_mbar_init(uint32_t mbar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void rag_mbar_inval(uint32_t mbar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(mbar) : "memory");
+}
+// Every thread, before the barrier that precedes a bulk copy: orders its
+// earlier generic accesses (the factors in shared memory, the cache slots in
+// global memory) before the async proxy's.
+__device__ __forceinline__ void rag_proxy_fence() { asm volatile("fence.proxy.async;" ::: "memory"); }
+// One thread: announce the bytes, start the copies.  Sizes are multiples of
+// 16 bytes, addresses 16-byte aligned.
+__device__ __forceinline__ void rag_bulk_issue2(uint32_t mbar, void* d0, const void* s0, uint32_t b0, void* d1,
+                                                const void* s1, uint32_t b1) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(b0 + b1) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   rag_smem_addr(d0)),
+               "l"(s0), "r"(b0), "r"(mbar)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   rag_smem_addr(d1)),
+               "l"(s1), "r"(b1), "r"(mbar)
+               : "memory");
+}
+// Waits for the mbarrier phase, for about one second of SM clock at most;
+// on expiry raises *err and returns false.
+__device__ __forceinline__ bool rag_mbar_wait(uint32_t mbar, uint32_t phase, unsigned int* err) {
+  const long long start = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if (clock64() - start > 2000000000ll) break;
+  }
+  atomicExch(err, 1u);
+  return false;
+}
+#endif
+
 constexpr int kRagMaxDim = 128;
 constexpr int kRagWarps = 8;  // warps per CTA
 constexpr int kRagClasses = 4;
@@ -80,8 +132,8 @@ __host__ __device__ constexpr int rag_class_chunks(int c) { return c <= 1 ? 4 : 
 // factors ld*ld, pivot reciprocals ld, H 7*ld, HH 7*ld, staging ld, params
 // ld/2+2, permutation ld/2 (ld ints), cache table 48 (16 keys, 16 stamps,
 // 16 states), exchange area 80 (2 broadcast slots, 2 x 4 reduction values,
-// 2 x 4 reduction indices, the work item, 2 x 32 block values of the
-// substitutions).
+// 2 x 4 reduction indices, the bulk-copy mbarrier at 14, the work item at 15,
+// 2 x 32 block values of the substitutions from 16).
 struct RagSmem {
   __host__ __device__ static constexpr int M(int) { return 0; }
   __host__ __device__ static constexpr int rinv(int ld) { return ld * ld; }
@@ -146,6 +198,7 @@ struct RaggedArgs {
   double* gcache;              // per CTA rag_gcache_cta_doubles()
   unsigned long long* queues;  // [kRagClasses] work counters, zero at launch
   unsigned long long* first_fail;
+  unsigned int* error_flag;    // raised when a bounded wait on a bulk copy gives up
 };
 
 // Damped spring-mass chain (unit masses): rows 0..N-1 are x' = v, rows
@@ -186,6 +239,9 @@ struct RagGroup {
   int nchunk;    // chunks per 32-row block (0 for a one-warp group)
   double* xch;   // exchange area (RagSmem::xch)
   int par;       // parity of the next reduction's buffer
+  uint32_t mbar;   // the group's mbarrier for bulk copies (shared address)
+  uint32_t mphase; // its next phase parity
+  unsigned int* err;  // raised when a bounded wait gives up
 
   // Producer/consumer hand-off on a named barrier: the producing warp
   // arrives (and moves on), the consuming warps wait.  cnt counts both.
@@ -220,12 +276,14 @@ struct RagGroup {
     for (int w = 1; w < nthr / 32; ++w) s = O::add(s, red[w]);
     return s;
   }
-  // arg-max of (value, index) with the lowest index winning ties; NaN values
-  // never win
-  __device__ __forceinline__ int argmax(double v, int idx) {
+  // arg-max of (magnitude, index) with the lowest index winning ties, for
+  // magnitudes that are non-negative and not NaN, given as their bit
+  // patterns: integer order is then numeric order, and the compares stay off
+  // the FP64 pipe
+  __device__ __forceinline__ int argmax_bits(unsigned long long v, int idx) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, off);
       const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
       if (ov > v || (ov == v && oi < idx)) {
         v = ov;
@@ -233,7 +291,7 @@ struct RagGroup {
       }
     }
     if (nthr == 32) return idx;
-    double* red = xch + 2 + 4 * par;
+    unsigned long long* red = reinterpret_cast<unsigned long long*>(xch + 2 + 4 * par);
     int* redi = reinterpret_cast<int*>(xch + 10) + 4 * par;
     if ((t & 31) == 0) {
       red[t >> 5] = v;
@@ -241,7 +299,7 @@ struct RagGroup {
     }
     par ^= 1;
     sync();
-    double bv = red[0];
+    unsigned long long bv = red[0];
     int bi = redi[0];
     for (int w = 1; w < nthr / 32; ++w)
       if (red[w] > bv || (red[w] == bv && redi[w] < bi)) {
@@ -267,19 +325,23 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
   g.sync();
   for (int i = 0; i < D; ++i) {
     double* col = M + i * D;
-    const double diag = fabs(col[i]);
+    // pivot: the first row of maximum |M[r][i]| from the diagonal down (a NaN
+    // below the diagonal never wins, a NaN diagonal stays), on the magnitudes'
+    // bit patterns
+    constexpr unsigned long long kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
+    const unsigned long long diag = static_cast<unsigned long long>(__double_as_longlong(col[i])) & kAbs;
     int pr = i;
-    if (diag == diag) {
-      double v = diag;
+    if (diag <= kInf) {
+      unsigned long long v = diag;
       int idx = i;
       if (r > i && r < D) {
-        const double a = fabs(col[r]);
-        if (a > diag) {
+        const unsigned long long a = static_cast<unsigned long long>(__double_as_longlong(col[r])) & kAbs;
+        if (a > diag && a <= kInf) {
           v = a;
           idx = r;
         }
       }
-      pr = g.argmax(v, idx);
+      pr = g.argmax_bits(v, idx);
     }
     if (pr != i) {
       for (int k = r; k < D; k += g.nthr) {
@@ -295,15 +357,45 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
       g.sync();
     }
     const double piv = col[i];
-    if (piv == 0.0) return false;
+    if ((static_cast<unsigned long long>(__double_as_longlong(piv)) & kAbs) == 0ull) return false;  // piv == 0
     const double inv = O::div(1.0, piv);
     if (r == 0) rinv[i] = inv;
-    if (r > i && r < D) {
-      const double l = O::mul(col[r], inv);
-      col[r] = l;
-      for (int k = i + 1; k < D; ++k) {
-        double* ck = M + k * D;
-        ck[r] = __fma_rn(-l, ck[i], ck[r]);
+    if (r > i && r < D) col[r] = O::mul(col[r], inv);
+    const int m = D - 1 - i;  // rows (and columns) below / right of the pivot
+    if (m > 0) {
+      g.sync();  // the multipliers
+      // Trailing update, balanced over the whole group: columns dealt
+      // round-robin to the warps, the m rows to the lanes (up to four each,
+      // independent FMAs).  Every element receives the same FMA in the same
+      // pivot order as with one row per thread.
+      const int w = r >> 5, lane = r & 31, nw = g.nthr >> 5;
+      const double* lc = col + i + 1;
+      const double l0 = lane < m ? lc[lane] : 0.0;
+      const double l1 = lane + 32 < m ? lc[lane + 32] : 0.0;
+      const double l2 = lane + 64 < m ? lc[lane + 64] : 0.0;
+      const double l3 = lane + 96 < m ? lc[lane + 96] : 0.0;
+      int k = i + 1 + w;
+      for (; k + nw < D; k += 2 * nw) {  // two columns at a time, loads first
+        double* c0 = M + k * D + i + 1;
+        double* c1 = c0 + nw * D;
+        const double u0 = c0[-1], u1 = c1[-1];  // U[i][k], U[i][k + nw]
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0;
+        if (lane < m) { a0 = c0[lane]; b0 = c1[lane]; }
+        if (lane + 32 < m) { a1 = c0[lane + 32]; b1 = c1[lane + 32]; }
+        if (lane + 64 < m) { a2 = c0[lane + 64]; b2 = c1[lane + 64]; }
+        if (lane + 96 < m) { a3 = c0[lane + 96]; b3 = c1[lane + 96]; }
+        if (lane < m) { c0[lane] = __fma_rn(-l0, u0, a0); c1[lane] = __fma_rn(-l0, u1, b0); }
+        if (lane + 32 < m) { c0[lane + 32] = __fma_rn(-l1, u0, a1); c1[lane + 32] = __fma_rn(-l1, u1, b1); }
+        if (lane + 64 < m) { c0[lane + 64] = __fma_rn(-l2, u0, a2); c1[lane + 64] = __fma_rn(-l2, u1, b2); }
+        if (lane + 96 < m) { c0[lane + 96] = __fma_rn(-l3, u0, a3); c1[lane + 96] = __fma_rn(-l3, u1, b3); }
+      }
+      if (k < D) {
+        double* ck = M + k * D + i + 1;
+        const double u = ck[-1];
+        if (lane < m) ck[lane] = __fma_rn(-l0, u, ck[lane]);
+        if (lane + 32 < m) ck[lane + 32] = __fma_rn(-l1, u, ck[lane + 32]);
+        if (lane + 64 < m) ck[lane + 64] = __fma_rn(-l2, u, ck[lane + 64]);
+        if (lane + 96 < m) ck[lane + 96] = __fma_rn(-l3, u, ck[lane + 96]);
       }
     }
     g.sync();
@@ -360,11 +452,18 @@ __device__ __forceinline__ int rag_get_factors(RagGroup& g, int D, int N, const 
   if (hit >= 0) {
     const int st = states[hit];
     if (st == 1) {
+      // factors and reciprocals by one bulk copy each (D is even, so both
+      // sizes are multiples of 16 bytes), the permutation by plain loads
       const double* gs = gcache + hit * slot_doubles;
-      rag_copy(g, sM, gs, D * D);
-      rag_copy(g, srinv, gs + static_cast<size_t>(gld) * gld, D);
+      rag_proxy_fence();
+      g.sync();  // every earlier access of the factors and the slots is done
+      if (g.t == 0)
+        rag_bulk_issue2(g.mbar, sM, gs, static_cast<uint32_t>(D * D * 8), srinv, gs + static_cast<size_t>(gld) * gld,
+                        static_cast<uint32_t>(D * 8));
       const int32_t* gp = reinterpret_cast<const int32_t*>(gs + static_cast<size_t>(gld) * gld + gld);
       for (int r = g.t; r < D; r += g.nthr) sperm[r] = gp[r];
+      rag_mbar_wait(g.mbar, g.mphase, g.err);
+      g.mphase ^= 1u;
     }
     g.sync();
     if (g.t == 0) stamps[hit] = cache.clock;
@@ -741,6 +840,11 @@ __global__ void __launch_bounds__(kRagWarps * 32, 1)
       g.cbar = 1 + rag_class_groups(c) + grp * g.nchunk;
       g.xch = ws + RagSmem::xch(ld);
       g.par = 0;
+      g.mbar = rag_smem_addr(g.xch + 14);
+      g.mphase = 0u;
+      g.err = rg.error_flag;
+      if (g.t == 0) rag_mbar_init(g.mbar);
+      g.sync();
       double* gcache = gcache_cta + static_cast<size_t>(grp) * rag_gcache_group_doubles(c);
       unsigned long long* slot = reinterpret_cast<unsigned long long*>(g.xch + 15);
       for (;;) {
@@ -752,6 +856,8 @@ __global__ void __launch_bounds__(kRagWarps * 32, 1)
         const int64_t idx = static_cast<int64_t>(rg.order[rg.class_start[c] + static_cast<int64_t>(item)]);
         rag_solve_system(rg, idx, g, ws, ld, gcache);
       }
+      g.sync();
+      if (g.t == 0) rag_mbar_inval(g.mbar);  // before the next phase reuses this memory
     }
     __syncthreads();
   }

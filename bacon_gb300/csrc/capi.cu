@@ -1135,6 +1135,7 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   rg.qmax = a.qmax;
   rg.queues = c->d_ctl + 8;
   rg.first_fail = c->d_ctl + 5;
+  rg.error_flag = reinterpret_cast<unsigned int*>(c->d_ctl + 6);
   for (int cl = 0, start = 0; cl < bacon::kRagClasses; start += static_cast<int>(class_n[cl]), ++cl) {
     rg.class_start[cl] = start;
     rg.class_n[cl] = class_n[cl];
@@ -1223,6 +1224,7 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
   BACON_CUDA(cudaMemsetAsync(c->d_ctl + 8, 0, bacon::kRagClasses * sizeof(unsigned long long), c->stream));
   BACON_CUDA(cudaMemsetAsync(c->d_ctl + 5, 0xff, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 6, 0, sizeof(unsigned long long), c->stream));
   void* args[] = {&a, &dyn, &rg};
   BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
   BACON_CUDA(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(block), args, smem, c->stream));
@@ -1238,12 +1240,13 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   }
   BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
-  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 5, c->d_ctl + 5, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 5, c->d_ctl + 5, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
   c->launches += 1;
   c->ev_valid = true;
   BACON_CUDA(cudaStreamSynchronize(c->stream));
   BACON_CUDA(cudaGetLastError());
+  if (c->h_ctl[6] != 0) return fail(BACON_CUDA_ERROR, "ragged BDF: a bounded wait on a factor copy gave up");
   const unsigned long long gf = c->h_ctl[5];
   if (gn > 0 && gf != ~0ull) {
     int32_t st = 0;
