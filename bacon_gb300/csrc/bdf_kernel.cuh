@@ -178,6 +178,37 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
   for (int r = 0; r < D; ++r)
 #pragma unroll
     for (int k = r + 1; k < D; ++k) M[r][k] = O::mul(M[r][k], rinv[r]);
+  // the unit factors replaced by their inverses (strict parts in place; one
+  // block of the 32-row blocked solve), column c the solve of e_c with every
+  // update taken for every column
+  {
+    double T[D][D];
+#pragma unroll
+    for (int cc = 0; cc < D; ++cc) {
+      double x[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = (j == cc) ? 1.0 : 0.0;
+#pragma unroll
+      for (int k = 0; k + 1 < D; ++k)
+#pragma unroll
+        for (int j = k + 1; j < D; ++j) x[j] = __fma_rn(-M[j][k], x[k], x[j]);
+#pragma unroll
+      for (int j = cc + 1; j < D; ++j) T[j][cc] = x[j];
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = (j == cc) ? 1.0 : 0.0;
+#pragma unroll
+      for (int k = D - 1; k > 0; --k)
+#pragma unroll
+        for (int j = 0; j < k; ++j) x[j] = __fma_rn(-M[j][k], x[k], x[j]);
+#pragma unroll
+      for (int j = 0; j < cc; ++j) T[j][cc] = x[j];
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+#pragma unroll
+      for (int cc = 0; cc < D; ++cc)
+        if (j != cc) M[j][cc] = T[j][cc];
+  }
   const double conv = O::mul(1e-3, tol);
   for (int it = 0; it < max_newton; ++it) {
     double f[D], dx[D];
@@ -197,16 +228,29 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
         dx[i] = b;
       }
     }
+    {
+      // x = Linv r (ascending k), then the reciprocals, then x = Uinv r
+      // (descending k)
+      double rb[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) rb[j] = dx[j];
 #pragma unroll
-      for (int r = i + 1; r < D; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
+      for (int j = 0; j < D; ++j) {
+        double acc = rb[j];
 #pragma unroll
-    for (int r = 0; r < D; ++r) dx[r] = O::mul(dx[r], rinv[r]);
+        for (int k = 0; k < j; ++k) acc = __fma_rn(M[j][k], rb[k], acc);
+        dx[j] = acc;
+      }
 #pragma unroll
-    for (int i = D - 1; i > 0; --i)
+      for (int j = 0; j < D; ++j) rb[j] = O::mul(dx[j], rinv[j]);
 #pragma unroll
-      for (int r = 0; r < i; ++r) dx[r] = __fma_rn(-M[r][i], dx[i], dx[r]);
+      for (int j = 0; j < D; ++j) {
+        double acc = rb[j];
+#pragma unroll
+        for (int k = D - 1; k > j; --k) acc = __fma_rn(M[j][k], rb[k], acc);
+        dx[j] = acc;
+      }
+    }
     double dn = 0.0;
 #pragma unroll
     for (int d = 0; d < D; ++d) {

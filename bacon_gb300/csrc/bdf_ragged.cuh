@@ -9,12 +9,13 @@
 // conflict-free read across the group), the pivot reciprocals and the row
 // permutation, the history H[0..6], the interpolated history HH, a staging
 // vector, the parameters and a small exchange area for broadcasts and
-// reductions.  The substitutions go by 32-row blocks: the block's warp runs
-// its triangle with shuffles (the dependent chain over the pivots stays
-// inside one warp) and publishes the values in chunks of 8 or 16 through
-// shared memory, arriving on a named barrier per chunk without waiting; the
-// warps below wait on it and apply each chunk while the block's warp
-// continues, so the next block's warp starts its triangle almost at once.
+// reductions.  The substitutions go by 32-row blocks whose diagonal blocks
+// hold their own inverses: the block's warp forms the product of the inverse
+// with its complete right-hand side (staged in shared memory; no dependent
+// chain over the pivots) and publishes the values in chunks of 8 or 16,
+// arriving on a named barrier per chunk without waiting; the warps below wait
+// on it and apply each chunk while the block's warp continues, so the next
+// block's warp starts its product almost at once.
 //
 // Factors are costly to recompute (2/3 dim^3 flops) and the chain Jacobian is
 // constant, so M depends on h b_q alone.  A solve meets ~100 distinct values
@@ -39,10 +40,14 @@
 //     arg-max with lowest-index ties), whole-row swaps, l = M[r][i] * (1 /
 //     M[i][i]), M[r][k] = fma(-l, M[i][k], M[r][k]) pivot by pivot;
 //   - the rows of U are then scaled by the pivot reciprocals the elimination
-//     formed (a unit upper factor, so no product sits on the back
-//     substitution's chain); the back substitution scales its right-hand
-//     side by them once;
-//   - substitutions: row r receives its fused updates in pivot order; the
+//     formed (a unit upper factor); the back substitution scales its
+//     right-hand side by them once;
+//   - each 32x32 diagonal block of L and of the scaled U is replaced by its
+//     inverse (column c = the solve of e_c, every update taken for every
+//     column in the oracle's order);
+//   - substitutions: row r receives the fused updates from the other blocks
+//     in pivot order, then the product with its block's inverse accumulates
+//     onto it in ascending (L) or descending (U) column order; the
 //     permutation is applied as one gather (it only moves values);
 //   - the Newton step norm and the error norm only feed comparisons with
 //     thresholds: a group tree sum decides them unless it lies within 1e-10
@@ -131,9 +136,10 @@ __host__ __device__ constexpr int rag_class_chunks(int c) { return c <= 1 ? 4 : 
 // One group's shared-memory slice for systems of dim <= ld, in doubles:
 // factors ld*ld, pivot reciprocals ld, H 7*ld, HH 7*ld, staging ld, params
 // ld/2+2, permutation ld/2 (ld ints), cache table 48 (16 keys, 16 stamps,
-// 16 states), exchange area 80 (2 broadcast slots, 2 x 4 reduction values,
+// 16 states), exchange area (2 broadcast slots, 2 x 4 reduction values,
 // 2 x 4 reduction indices, the bulk-copy mbarrier at 14, the work item at 15,
-// 2 x 32 block values of the substitutions from 16).
+// 2 x 32 block values of the substitutions from 16, the producing block's
+// right-hand side from 80; 112 in all).
 struct RagSmem {
   __host__ __device__ static constexpr int M(int) { return 0; }
   __host__ __device__ static constexpr int rinv(int ld) { return ld * ld; }
@@ -144,7 +150,7 @@ struct RagSmem {
   __host__ __device__ static constexpr int perm(int ld) { return ld * ld + 16 * ld + ld / 2 + 2; }
   __host__ __device__ static constexpr int table(int ld) { return perm(ld) + ld / 2; }
   __host__ __device__ static constexpr int xch(int ld) { return table(ld) + 48; }
-  __host__ __device__ static constexpr int doubles(int ld) { return xch(ld) + 80; }
+  __host__ __device__ static constexpr int doubles(int ld) { return xch(ld) + 112; }
 };
 
 // Shared memory of a CTA for the classes present (bit c of mask = class c).
@@ -401,10 +407,52 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
     g.sync();
   }
   // the rows of U scaled by their pivot reciprocal (a unit upper factor for
-  // the back substitution); the caller syncs before the factors are read
+  // the back substitution)
   if (r < D) {
     const double s = rinv[r];
     for (int k = r + 1; k < D; ++k) M[k * D + r] = O::mul(M[k * D + r], s);
+  }
+  // The diagonal 32-row blocks of L and of the scaled U replaced by their
+  // inverses (strict parts in place): block b by warp b (its own rows), lane
+  // c computing column c as the solve of e_c, every update taken for every
+  // column in the oracle's order.  The caller syncs before the factors are
+  // read.
+  const int nw = g.nthr >> 5, lane = r & 31;
+  for (int b = r >> 5; b * 32 < D; b += nw) {
+    __syncwarp();
+    const int s0 = 32 * b;
+    const int nb = min(32, D - s0);
+    double* blk = M + s0 * D + s0;  // element (j, k) of the block at blk[k * D + j]
+    double x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = (j == lane) ? 1.0 : 0.0;
+#pragma unroll
+    for (int k = 0; k < 31; ++k)
+      if (k + 1 < nb) {
+#pragma unroll
+        for (int j = k + 1; j < 32; ++j)
+          if (j < nb) x[j] = __fma_rn(-blk[k * D + j], x[k], x[j]);
+      }
+    __syncwarp();  // every lane has read the lower block
+    if (lane < nb) {
+#pragma unroll
+      for (int j = 1; j < 32; ++j)
+        if (j > lane && j < nb) blk[lane * D + j] = x[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = (j == lane) ? 1.0 : 0.0;
+#pragma unroll
+    for (int k = 31; k > 0; --k)
+      if (k < nb) {
+#pragma unroll
+        for (int j = 0; j < k; ++j) x[j] = __fma_rn(-blk[k * D + j], x[k], x[j]);
+      }
+    __syncwarp();  // every lane has read the upper block
+    if (lane < nb) {
+#pragma unroll
+      for (int j = 0; j < 31; ++j)
+        if (j < lane) blk[lane * D + j] = x[j];
+    }
   }
   return true;
 }
@@ -538,6 +586,7 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
     const int wg = r >> 5, lane = r & 31;
     const int nblk = (D + 31) >> 5;
     double* xs = g.xch + 16;  // [2][32], alternating blocks
+    double* rin = g.xch + 80;  // the producing block's right-hand side
     const int cs = g.nchunk > 0 ? 32 / g.nchunk : 32;
     // forward, unit lower factor
     for (int b = 0; b < nblk; ++b) {
@@ -546,11 +595,24 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
       const unsigned cnt = 32u * static_cast<unsigned>(nblk - b);
       double* xb = xs + (b & 1) * 32;
       if (wg == b) {
+        // x = Linv r: lane j adds Linv[j][k] r_k for k < j, ascending.  The
+        // right-hand side is complete, so it is staged once in shared memory
+        // and read back as broadcasts (a shuffle per term would cost ~50
+        // cycles more per FMA)
+        rin[lane] = dx;
+        __syncwarp();
         for (int lo = 0; lo < nb; lo += cs) {
           const int hi = min(lo + cs, nb);
-          for (int ii = lo; ii < hi && ii + 1 < nb; ++ii) {
-            const double xi = __shfl_sync(0xffffffffu, dx, ii);
-            if (lane > ii && own) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+          for (int k0 = lo; k0 < hi; k0 += 8) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int k = k0 + q;
+              if (k < hi) {
+                const double m = own ? M[(base + k) * D + r] : 0.0;
+                const double rk = rin[k];
+                if (lane > k && own) dx = __fma_rn(m, rk, dx);
+              }
+            }
           }
           if (b + 1 < nblk) {
             if (lane >= lo && lane < hi) xb[lane] = dx;
@@ -562,16 +624,22 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
           const int hi = min(lo + cs, nb);
           g.wait(g.cbar + lo / cs, cnt);
           if (own)
-            for (int ii = lo; ii < hi; ++ii) dx = __fma_rn(-M[(base + ii) * D + r], xb[ii], dx);
+            for (int k0 = lo; k0 < hi; k0 += 8) {
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {
+                const int k = k0 + q;
+                if (k < hi) dx = __fma_rn(-M[(base + k) * D + r], xb[k], dx);
+              }
+            }
         }
       }
     }
     // back, on the row-scaled unit upper factor.  The group sync closes every
-    // forward chunk phase first: warp 0 only arrived on block 0's chunk
-    // barriers, and its waits below use the same ids.  It costs no time on
-    // the critical path (the last block's warp finishes the forward last and
-    // starts the back first).
-    if (nblk > 1) g.sync();
+    // forward chunk phase first (warp 0 only arrived on block 0's chunk
+    // barriers, and its waits below use the same ids) and every read of the
+    // staged right-hand side.  It costs no time on the critical path (the
+    // last block's warp finishes the forward last and starts the back first).
+    g.sync();
     if (own) dx = O::mul(dx, srinv[r]);
     for (int b = nblk - 1; b >= 0; --b) {
       const int base = 32 * b;
@@ -579,11 +647,21 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
       const unsigned cnt = 32u * static_cast<unsigned>(b + 1);
       double* xb = xs + (b & 1) * 32;
       if (wg == b) {
+        // x = Uinv r: lane j adds Uinv[j][k] r_k for k > j, descending
+        rin[lane] = dx;
+        __syncwarp();
         for (int hi = nb; hi > 0; hi -= cs) {
           const int lo = max(hi - cs, 0);
-          for (int ii = hi - 1; ii >= lo && ii > 0; --ii) {
-            const double xi = __shfl_sync(0xffffffffu, dx, ii);
-            if (lane < ii) dx = __fma_rn(-M[(base + ii) * D + r], xi, dx);
+          for (int k1 = hi - 1; k1 >= lo; k1 -= 8) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int k = k1 - q;
+              if (k >= lo) {
+                const double m = own ? M[(base + k) * D + r] : 0.0;
+                const double rk = rin[k];
+                if (lane < k) dx = __fma_rn(m, rk, dx);
+              }
+            }
           }
           if (b > 0) {
             if (lane >= lo && lane < hi) xb[lane] = dx;
@@ -594,7 +672,13 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
         for (int hi = nb; hi > 0; hi -= cs) {
           const int lo = max(hi - cs, 0);
           g.wait(g.cbar + (nb - hi) / cs, cnt);
-          for (int ii = hi - 1; ii >= lo; --ii) dx = __fma_rn(-M[(base + ii) * D + r], xb[ii], dx);
+          for (int k1 = hi - 1; k1 >= lo; k1 -= 8) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int k = k1 - q;
+              if (k >= lo) dx = __fma_rn(-M[(base + k) * D + r], xb[k], dx);
+            }
+          }
         }
       }
     }

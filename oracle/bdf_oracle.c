@@ -384,6 +384,38 @@ static const double kBdfA[7][6] = {
 int oracle_rhs_jacobian(int32_t rhs, int32_t dim, double t, const double* y, const double* p,
                         const double* shared, double* J /* row-major dim x dim */);
 
+/* The linear solves go by blocks of 32 rows.  After the LU, each diagonal
+ * block of L (unit lower) and of the row-scaled U (unit upper) is replaced by
+ * its inverse, strict parts in place (the unit diagonals stay implicit), so
+ * that a block's solve is one product with a right-hand side that is already
+ * complete rather than a chain of dependent updates.  Column c of an inverse
+ * is the solve of the unit vector e_c, every update taken for every column in
+ * the same order (updates by a zero leave a value unchanged, so this equals
+ * the solve restricted to its non-zero part, and NaN spreads the same way). */
+enum { kSolveBlock = 32 };
+
+static void block_inverses(int n, dmat M) {
+  double T[kSolveBlock][kSolveBlock], x[kSolveBlock];
+  for (int s = 0; s < n; s += kSolveBlock) {
+    const int nb = (n - s < kSolveBlock) ? n - s : kSolveBlock;
+    for (int c = 0; c < nb; ++c) { /* L_bb^-1 e_c: forward, unit diagonal */
+      for (int j = 0; j < nb; ++j) x[j] = (j == c) ? 1.0 : 0.0;
+      for (int k = 0; k + 1 < nb; ++k)
+        for (int j = k + 1; j < nb; ++j) x[j] = fma(-M[s + j][s + k], x[k], x[j]);
+      for (int j = c + 1; j < nb; ++j) T[j][c] = x[j];
+    }
+    for (int c = 0; c < nb; ++c) { /* U_bb^-1 e_c: backward, unit diagonal */
+      for (int j = 0; j < nb; ++j) x[j] = (j == c) ? 1.0 : 0.0;
+      for (int k = nb - 1; k > 0; --k)
+        for (int j = 0; j < k; ++j) x[j] = fma(-M[s + j][s + k], x[k], x[j]);
+      for (int j = 0; j < c; ++j) T[j][c] = x[j];
+    }
+    for (int j = 0; j < nb; ++j)
+      for (int c = 0; c < nb; ++c)
+        if (j != c) M[s + j][s + c] = T[j][c];
+  }
+}
+
 /* Solve G(y) = y - dt*b*f(t1, y) + sum_j a_j H[j-1] = 0 by Newton with the
  * Jacobian at the initial guess (one LU).  Returns 1 on convergence. */
 static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const double* p,
@@ -428,6 +460,7 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
    * then runs on a unit upper factor, with no product on its critical path */
   for (int r = 0; r < n; ++r)
     for (int k = r + 1; k < n; ++k) M[r][k] = M[r][k] * rinv[r];
+  block_inverses(n, M);
   const int max_newton = cfg->max_iter > 0 ? cfg->max_iter : 8;
   for (int it = 0; it < max_newton; ++it) {
     oracle_rhs(rhs, n, t1, y, p, shared, f);
@@ -436,13 +469,38 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
     for (int d = 0; d < n; ++d) dx[d] = -g[d];
     for (int i = 0; i < n; ++i)
       if (piv[i] != i) { const double t = dx[i]; dx[i] = dx[piv[i]]; dx[piv[i]] = t; }
-    for (int i = 0; i < n; ++i)
-      for (int r = i + 1; r < n; ++r) dx[r] = fma(-M[r][i], dx[i], dx[r]);
-    /* back substitution on the row-scaled upper factor: the right-hand side
-     * takes the pivot reciprocals first (the elimination's own, no division) */
+    /* forward, block by block: the updates from earlier blocks in pivot
+     * order, then the product with the block's inverse, x_j = r_j +
+     * sum_{k<j} Linv[j][k] r_k in ascending k */
+    for (int s = 0; s < n; s += kSolveBlock) {
+      const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
+      for (int r = s; r < e; ++r)
+        for (int k = 0; k < s; ++k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
+      double rb[kSolveBlock];
+      for (int j = s; j < e; ++j) rb[j - s] = dx[j];
+      for (int j = s; j < e; ++j) {
+        double acc = rb[j - s];
+        for (int k = s; k < j; ++k) acc = fma(M[j][k], rb[k - s], acc);
+        dx[j] = acc;
+      }
+    }
+    /* back, on the row-scaled upper factor: the right-hand side takes the
+     * pivot reciprocals first (the elimination's own, no division); per block
+     * from the last, the updates from later blocks in descending pivot order,
+     * then x_j = r_j + sum_{k>j} Uinv[j][k] r_k in descending k */
     for (int r = 0; r < n; ++r) dx[r] = dx[r] * rinv[r];
-    for (int i = n - 1; i > 0; --i)
-      for (int r = 0; r < i; ++r) dx[r] = fma(-M[r][i], dx[i], dx[r]);
+    for (int s = ((n - 1) / kSolveBlock) * kSolveBlock; s >= 0; s -= kSolveBlock) {
+      const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
+      for (int r = s; r < e; ++r)
+        for (int k = n - 1; k >= e; --k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
+      double rb[kSolveBlock];
+      for (int j = s; j < e; ++j) rb[j - s] = dx[j];
+      for (int j = s; j < e; ++j) {
+        double acc = rb[j - s];
+        for (int k = e - 1; k > j; --k) acc = fma(M[j][k], rb[k - s], acc);
+        dx[j] = acc;
+      }
+    }
     double dn = 0.0;
     for (int d = 0; d < n; ++d) {
       y[d] = y[d] + dx[d];
