@@ -141,6 +141,23 @@ __device__ __forceinline__ void ad_pd_pop_front(AdamsState<O, D>& s) {
   s.npd--;
 }
 
+// Entry i (< L) of prev_values, i known only at run time: a chain of selects
+// over the compile-time positions.  (A predicated copy inside a loop lets the
+// compiler turn the deques into indexed local memory, on every step's path.)
+template <int L, int O, int D>
+__device__ __forceinline__ void ad_pv_select(const AdamsState<O, D>& s, int i, double& t, double (&y)[D]) {
+  t = s.pv_t[0];
+#pragma unroll
+  for (int d = 0; d < D; ++d) y[d] = s.pv_y[0][d];
+#pragma unroll
+  for (int k = 1; k < L; ++k) {
+    const bool hit = (k == i);
+    t = hit ? s.pv_t[k] : t;
+#pragma unroll
+    for (int d = 0; d < D; ++d) y[d] = hit ? s.pv_y[k][d] : y[d];
+  }
+}
+
 // AdamsSolver::runge_kutta (src/ivp/adams.rs:344-395).
 template <int O, class Rhs>
 __device__ __forceinline__ void ad_runge_kutta(AdamsState<O, Rhs::DIM>& s, const double* p, int iterations) {
@@ -197,13 +214,7 @@ __device__ __forceinline__ int ad_step(AdamsState<O, Rhs::DIM>& s, const double*
     const int get_item = O - s.yield_memory - 1;
     s.yield_memory -= 1;
     if (s.yield_memory == 0) s.yield_memory = O + 1;
-#pragma unroll
-    for (int i = 0; i < O; ++i)
-      if (i == get_item) {
-        it = s.pv_t[i];
-#pragma unroll
-        for (int d = 0; d < D; ++d) iy[d] = s.pv_y[i][d];
-      }
+    ad_pv_select<O>(s, get_item, it, iy);
     return kAdItem;
   }
   if (s.yield_memory == O + 1) {
@@ -219,12 +230,9 @@ __device__ __forceinline__ int ad_step(AdamsState<O, Rhs::DIM>& s, const double*
   if (X::add(s.time, s.dt) >= s.end) {
     s.dt = X::sub(s.end, s.time);
     ad_runge_kutta<O, Rhs>(s, p, 1);
+    double back_t;
+    ad_pv_select<AdamsState<O, D>::kCap>(s, s.npv - 1, back_t, iy);
     it = s.time;
-#pragma unroll
-    for (int i = 0; i < AdamsState<O, D>::kCap; ++i)
-      if (i == s.npv - 1)
-#pragma unroll
-        for (int d = 0; d < D; ++d) iy[d] = s.pv_y[i][d];
     return kAdItem;
   }
   if (s.npv == 0) {

@@ -243,9 +243,12 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
         "value": vb.n / (ams * 1e-3), "unit": "solves/s", "kernel_ms": ams,
         "status_counts": {int(k): int((st == k).sum()) for k in np.unique(st)},
         "step_calls_mean": float((a5.accepted.double() + a5.rejected.double()).mean().item()),
+        "step_calls_max": float((a5.accepted.double() + a5.rejected.double()).max().item()),
         "note": "the reference's Adams5 restarts from an RK4 bootstrap after every dt change (~7e5 step calls "
-                "per system here) and 4096 one-thread systems fill 32 of 152 SMs: each thread runs its steps "
-                "serially, so a larger batch, not this one, is where the GPU pays off"}
+                "per system on average here, step_calls_max for the slowest) and one thread runs each system's "
+                "steps serially, each dependent FP64 operation ~64 cycles: the launch lasts as long as the slowest "
+                "system, and 4096 systems fill 32 of 152 SMs, so a larger batch, not this one, is where the GPU "
+                "pays off"}
 
     # Linear y' = A y, shared A (n = 256), 65,536 states, tol 1e-8.
     lb = W.linear_shared()
