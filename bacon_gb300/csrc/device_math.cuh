@@ -48,6 +48,28 @@ __device__ __forceinline__ uint32_t nonfinite_mask(const double (&v)[D]) {
   return m;
 }
 
+// Compares off the FP64 pipe.  The left operand is a norm, a ratio of
+// norms or a step size: non-negative (never -0) or NaN; the right one is
+// a positive tolerance, step bound or constant, or NaN.  For such values the
+// integer order of the bit patterns is the numeric order, and with the NaN
+// cases excluded explicitly each helper returns exactly the IEEE result.
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+__device__ __forceinline__ unsigned long long nn_bits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x));
+}
+__device__ __forceinline__ bool nn_le(double a, double b) {  // a <= b
+  return nn_bits(a) <= nn_bits(b) && nn_bits(b) <= kInfBits;
+}
+__device__ __forceinline__ bool nn_lt(double a, double b) {  // a < b
+  return nn_bits(a) < nn_bits(b) && nn_bits(b) <= kInfBits;
+}
+__device__ __forceinline__ bool nn_ge(double a, double b) {  // a >= b
+  return nn_bits(a) >= nn_bits(b) && nn_bits(a) <= kInfBits && nn_bits(b) <= kInfBits;
+}
+__device__ __forceinline__ bool nn_gt(double a, double b) {  // a > b
+  return nn_bits(a) > nn_bits(b) && nn_bits(a) <= kInfBits && nn_bits(b) <= kInfBits;
+}
+
 // One correction of r toward the correctly rounded x^(1/4): the residual
 // x - r^4 is formed in double-double and compared with the distance to the
 // neighbouring rounding midpoints (times 4 r^3).  The same operation
@@ -64,8 +86,14 @@ __device__ __forceinline__ double qrt_fix(double x, double r) {
   const double half_ulp = __longlong_as_double(static_cast<long long>((e - 53ull) << 52));
   const double thr_up = __dmul_rn(__dmul_rn(4.0, half_ulp), __dmul_rn(p_hi, r));
   const double thr_dn = ((rb & 0x000fffffffffffffull) == 0ull) ? __dmul_rn(0.5, thr_up) : thr_up;
-  if (res > thr_up) return __longlong_as_double(static_cast<long long>(rb + 1ull));
-  if (res < -thr_dn) return __longlong_as_double(static_cast<long long>(rb - 1ull));
+  // res > thr_up and res < -thr_dn on the bit patterns (res finite of either
+  // sign, the thresholds positive normal): a signed compare orders res
+  // against a positive value, and res < -thr_dn is a negative res of larger
+  // magnitude
+  const long long resb = __double_as_longlong(res);
+  if (resb > __double_as_longlong(thr_up)) return __longlong_as_double(static_cast<long long>(rb + 1ull));
+  if (resb < 0 && static_cast<unsigned long long>(resb & 0x7fffffffffffffffll) > nn_bits(thr_dn))
+    return __longlong_as_double(static_cast<long long>(rb - 1ull));
   return r;
 }
 
@@ -73,22 +101,28 @@ __device__ __forceinline__ double qrt_fix(double x, double r) {
 // (tol/err).powf(1/4), src/ivp/rk.rs:400-401).  Exact for the special values
 // pow() defines on this domain: +0 -> +0, +inf -> +inf, NaN -> NaN.
 __device__ __forceinline__ double qrt(double x) {
-  if (!(x > 0.0)) return (x == 0.0) ? 0.0 : __longlong_as_double(0x7ff8000000000000ll);
-  if (__double2hiint(x) == 0x7ff00000 && __double2loint(x) == 0) return x;  // +inf
+  // the special cases and the range split on the bit pattern (integer compares)
+  const long long xb = __double_as_longlong(x);
+  if (!(xb > 0 && xb <= static_cast<long long>(kInfBits)))  // !(x > 0): zeros, negatives, NaN
+    return ((xb & 0x7fffffffffffffffll) == 0) ? 0.0 : __longlong_as_double(0x7ff8000000000000ll);
+  if (xb == static_cast<long long>(kInfBits)) return x;  // +inf
   double s = 1.0;
-  if (x > 0x1p400) {
+  bool scaled = false;
+  if (xb > 0x58f0000000000000ll) {  // x > 2^400
     x = __dmul_rn(x, 0x1p-800);
     s = 0x1p200;
-  } else if (x < 0x1p-400) {
+    scaled = true;
+  } else if (xb < 0x26f0000000000000ll) {  // x < 2^-400
     x = __dmul_rn(x, 0x1p800);
     s = 0x1p-200;
+    scaled = true;
   }
   // sqrt(sqrt(x)) is within one ulp of x^(1/4): the inner rounding moves the
   // root by at most 2^-54 relative (half an ulp at the top of a binade) and
   // the outer rounding by half an ulp.  One correction therefore reaches the
   // correctly rounded value.
   const double r = qrt_fix(x, __dsqrt_rn(__dsqrt_rn(x)));
-  return __dmul_rn(r, s);
+  return scaled ? __dmul_rn(r, s) : r;
 }
 
 // One ulp-step correction of r ~ (z + adj)^(1/N), z in [1, 2^N), r in [1, 2):

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
       const double n2 = ff_to_double(n2f);
       const double tdt = __dmul_rn(tol, dt);
       const double thr = __dmul_rn(tdt, tdt);
-      const bool ok = n2 <= thr;
+      const bool ok = nn_le(n2, thr);  // squares of norms: >= 0 or NaN (integer compare)
 
       double tn = t;
       ff yn[D];
@@ -179,9 +179,9 @@ __global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
       if (delta <= 0.1f) dt = __dmul_rn(dt, 0.1);
       else if (delta >= 4.0f) dt = __dmul_rn(dt, 4.0);
       else dt = __dmul_rn(dt, static_cast<double>(delta));
-      if (dt > dt_max) dt = dt_max;
+      if (nn_gt(dt, dt_max)) dt = dt_max;  // dt >= 0 or NaN (integer compare)
 
-      if (dt < dt_min && (ok ? tn : t) < end) {
+      if (nn_lt(dt, dt_min) && (ok ? tn : t) < end) {
         fin = kStMinDt;
       } else if (ok) {
         if (a.traj_t != nullptr && acc < a.traj_cap) {

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
       });
       poison_components(ev, epoison);
       const double err = Ops::div(static_norm<Ops>(ev), dt);
-      const bool ok = err <= tol;
+      const bool ok = nn_le(err, tol);  // err >= 0 or NaN (integer compare)
 
       // Accept (rk.rs:392-398).
       double tn = t, yn[D];
@@ -235,12 +235,13 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
 
       // Controller (rk.rs:400-416); the safety factor is 100/100 = 1.
       const double delta = qrt(Ops::div(tol, err));
-      if (delta <= 0.1) dt = Ops::mul(dt, 0.1);
-      else if (delta >= 4.0) dt = Ops::mul(dt, 4.0);
+      // delta and dt are >= 0 or NaN: the compares run on the bit patterns
+      if (nn_le(delta, 0.1)) dt = Ops::mul(dt, 0.1);
+      else if (nn_ge(delta, 4.0)) dt = Ops::mul(dt, 4.0);
       else dt = Ops::mul(dt, delta);
-      if (dt > dt_max) dt = dt_max;
+      if (nn_gt(dt, dt_max)) dt = dt_max;
 
-      if (dt < dt_min && (ok ? tn : t) < end) {
+      if (nn_lt(dt, dt_min) && (ok ? tn : t) < end) {
         fin = kStMinDt;  // the accepted state of this attempt is never yielded
       } else if (kRecord && ok && acc >= a.max_steps) {
         fin = kStCapacity;  // the step log is full
