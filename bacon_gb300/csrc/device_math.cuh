@@ -82,10 +82,14 @@ __device__ __forceinline__ double qrt_fix(double x, double r) {
   q_lo = __fma_rn(__dmul_rn(2.0, p_hi), p_lo, q_lo);
   const double res = __dsub_rn(__dsub_rn(x, q_hi), q_lo);
   const unsigned long long rb = static_cast<unsigned long long>(__double_as_longlong(r));
-  const unsigned long long e = (rb >> 52) & 0x7ffull;
-  const double half_ulp = __longlong_as_double(static_cast<long long>((e - 53ull) << 52));
-  const double thr_up = __dmul_rn(__dmul_rn(4.0, half_ulp), __dmul_rn(p_hi, r));
-  const double thr_dn = ((rb & 0x000fffffffffffffull) == 0ull) ? __dmul_rn(0.5, thr_up) : thr_up;
+  const long long e = static_cast<long long>((rb >> 52) & 0x7ffull);
+  // thr_up = 4 * (half an ulp of r) * p_hi * r = RN(p_hi r) * 2^(e - 1074), e
+  // the biased exponent of r.  After qrt's range split r is in [2^-100,
+  // 2^100], so the power-of-two scaling stays in the normal range: it is
+  // exact, and done on the exponent field; so is the halving of thr_dn.
+  const double thr_up = __longlong_as_double(__double_as_longlong(__dmul_rn(p_hi, r)) + (e - 1074) * (1ll << 52));
+  const double thr_dn =
+      ((rb & 0x000fffffffffffffull) == 0ull) ? __longlong_as_double(__double_as_longlong(thr_up) - (1ll << 52)) : thr_up;
   // res > thr_up and res < -thr_dn on the bit patterns (res finite of either
   // sign, the thresholds positive normal): a signed compare orders res
   // against a positive value, and res < -thr_dn is a negative res of larger
