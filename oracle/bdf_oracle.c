@@ -416,25 +416,9 @@ static void block_inverses(int n, dmat M) {
   }
 }
 
-/* Solve G(y) = y - dt*b*f(t1, y) + sum_j a_j H[j-1] = 0 by Newton with the
- * Jacobian at the initial guess (one LU).  Returns 1 on convergence. */
-static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const double* p,
-                            const double* shared, double t1, double dt, int q,
-                            double H[][ORC_MAX_BDF_DIM], const double* guess0, double* y) {
-  static __thread double J[ORC_MAX_BDF_DIM * ORC_MAX_BDF_DIM];
-  static __thread dmat M;
-  double c[ORC_MAX_BDF_DIM], f[ORC_MAX_BDF_DIM], g[ORC_MAX_BDF_DIM], dx[ORC_MAX_BDF_DIM];
-  double rinv[ORC_MAX_BDF_DIM]; /* 1 / U[i][i], the elimination's own reciprocal */
-  int piv[ORC_MAX_BDF_DIM];
-  const double hb = dt * kBdfB[q];
-  /* constant part c = sum_j a_j H[j-1] */
-  for (int d = 0; d < n; ++d) c[d] = 0.0;
-  for (int j = 1; j <= q; ++j)
-    for (int d = 0; d < n; ++d) c[d] = c[d] + (kBdfA[q][j - 1] * H[j - 1][d]);
-  memcpy(y, guess0, sizeof(double) * n);
-  oracle_rhs_jacobian(rhs, n, t1, y, p, shared, J);
-  for (int r = 0; r < n; ++r)
-    for (int k = 0; k < n; ++k) M[r][k] = ((r == k) ? 1.0 : 0.0) - (hb * J[r * n + k]);
+/* Factors M in place for the corrected solve: the LU, the row-scaled U and
+ * the inverted diagonal blocks.  Returns 0 on an exactly zero pivot. */
+static int corrected_factor(int n, dmat M, int* piv, double* rinv) {
   /* LU with partial pivoting (first maximum), row swaps on the whole row.  The
    * elimination and both substitutions update with one fused multiply-add
    * (fma is correctly rounded, so every platform and the GPU agree): half the
@@ -461,46 +445,74 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
   for (int r = 0; r < n; ++r)
     for (int k = r + 1; k < n; ++k) M[r][k] = M[r][k] * rinv[r];
   block_inverses(n, M);
+  return 1;
+}
+
+/* Solves (the factored M) x = v in place in dx. */
+static void corrected_solve(int n, dmat M, const int* piv, const double* rinv, double* dx) {
+  for (int i = 0; i < n; ++i)
+    if (piv[i] != i) { const double t = dx[i]; dx[i] = dx[piv[i]]; dx[piv[i]] = t; }
+  /* forward, block by block: the updates from earlier blocks in pivot
+   * order, then the product with the block's inverse, x_j = r_j +
+   * sum_{k<j} Linv[j][k] r_k in ascending k */
+  for (int s = 0; s < n; s += kSolveBlock) {
+    const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
+    for (int r = s; r < e; ++r)
+      for (int k = 0; k < s; ++k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
+    double rb[kSolveBlock];
+    for (int j = s; j < e; ++j) rb[j - s] = dx[j];
+    for (int j = s; j < e; ++j) {
+      double acc = rb[j - s];
+      for (int k = s; k < j; ++k) acc = fma(M[j][k], rb[k - s], acc);
+      dx[j] = acc;
+    }
+  }
+  /* back, on the row-scaled upper factor: the right-hand side takes the
+   * pivot reciprocals first (the elimination's own, no division); per block
+   * from the last, the updates from later blocks in descending pivot order,
+   * then x_j = r_j + sum_{k>j} Uinv[j][k] r_k in descending k */
+  for (int r = 0; r < n; ++r) dx[r] = dx[r] * rinv[r];
+  for (int s = ((n - 1) / kSolveBlock) * kSolveBlock; s >= 0; s -= kSolveBlock) {
+    const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
+    for (int r = s; r < e; ++r)
+      for (int k = n - 1; k >= e; --k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
+    double rb[kSolveBlock];
+    for (int j = s; j < e; ++j) rb[j - s] = dx[j];
+    for (int j = s; j < e; ++j) {
+      double acc = rb[j - s];
+      for (int k = e - 1; k > j; --k) acc = fma(M[j][k], rb[k - s], acc);
+      dx[j] = acc;
+    }
+  }
+}
+
+/* Solve G(y) = y - dt*b*f(t1, y) + sum_j a_j H[j-1] = 0 by Newton with the
+ * Jacobian at the initial guess (one LU).  Returns 1 on convergence. */
+static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const double* p,
+                            const double* shared, double t1, double dt, int q,
+                            double H[][ORC_MAX_BDF_DIM], const double* guess0, double* y) {
+  static __thread double J[ORC_MAX_BDF_DIM * ORC_MAX_BDF_DIM];
+  static __thread dmat M;
+  double c[ORC_MAX_BDF_DIM], f[ORC_MAX_BDF_DIM], g[ORC_MAX_BDF_DIM], dx[ORC_MAX_BDF_DIM];
+  double rinv[ORC_MAX_BDF_DIM]; /* 1 / U[i][i], the elimination's own reciprocal */
+  int piv[ORC_MAX_BDF_DIM];
+  const double hb = dt * kBdfB[q];
+  /* constant part c = sum_j a_j H[j-1] */
+  for (int d = 0; d < n; ++d) c[d] = 0.0;
+  for (int j = 1; j <= q; ++j)
+    for (int d = 0; d < n; ++d) c[d] = c[d] + (kBdfA[q][j - 1] * H[j - 1][d]);
+  memcpy(y, guess0, sizeof(double) * n);
+  oracle_rhs_jacobian(rhs, n, t1, y, p, shared, J);
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) M[r][k] = ((r == k) ? 1.0 : 0.0) - (hb * J[r * n + k]);
+  if (!corrected_factor(n, M, piv, rinv)) return 0;
   const int max_newton = cfg->max_iter > 0 ? cfg->max_iter : 8;
   for (int it = 0; it < max_newton; ++it) {
     oracle_rhs(rhs, n, t1, y, p, shared, f);
     for (int d = 0; d < n; ++d) g[d] = (y[d] - (hb * f[d])) + c[d];
     /* solve M dx = -g */
     for (int d = 0; d < n; ++d) dx[d] = -g[d];
-    for (int i = 0; i < n; ++i)
-      if (piv[i] != i) { const double t = dx[i]; dx[i] = dx[piv[i]]; dx[piv[i]] = t; }
-    /* forward, block by block: the updates from earlier blocks in pivot
-     * order, then the product with the block's inverse, x_j = r_j +
-     * sum_{k<j} Linv[j][k] r_k in ascending k */
-    for (int s = 0; s < n; s += kSolveBlock) {
-      const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
-      for (int r = s; r < e; ++r)
-        for (int k = 0; k < s; ++k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
-      double rb[kSolveBlock];
-      for (int j = s; j < e; ++j) rb[j - s] = dx[j];
-      for (int j = s; j < e; ++j) {
-        double acc = rb[j - s];
-        for (int k = s; k < j; ++k) acc = fma(M[j][k], rb[k - s], acc);
-        dx[j] = acc;
-      }
-    }
-    /* back, on the row-scaled upper factor: the right-hand side takes the
-     * pivot reciprocals first (the elimination's own, no division); per block
-     * from the last, the updates from later blocks in descending pivot order,
-     * then x_j = r_j + sum_{k>j} Uinv[j][k] r_k in descending k */
-    for (int r = 0; r < n; ++r) dx[r] = dx[r] * rinv[r];
-    for (int s = ((n - 1) / kSolveBlock) * kSolveBlock; s >= 0; s -= kSolveBlock) {
-      const int e = (s + kSolveBlock < n) ? s + kSolveBlock : n;
-      for (int r = s; r < e; ++r)
-        for (int k = n - 1; k >= e; --k) dx[r] = fma(-M[r][k], dx[k], dx[r]);
-      double rb[kSolveBlock];
-      for (int j = s; j < e; ++j) rb[j - s] = dx[j];
-      for (int j = s; j < e; ++j) {
-        double acc = rb[j - s];
-        for (int k = e - 1; k > j; --k) acc = fma(M[j][k], rb[k - s], acc);
-        dx[j] = acc;
-      }
-    }
+    corrected_solve(n, M, piv, rinv, dx);
     double dn = 0.0;
     for (int d = 0; d < n; ++d) {
       y[d] = y[d] + dx[d];
@@ -642,4 +654,19 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
                            traj_t, traj_y, traj_cap);
   return bdf_corrected(cfg, rhs, dim, p, shared, t0, t_end, y0, y_out, t_out, accepted, rejected,
                        traj_t, traj_y, traj_cap);
+}
+
+/* The corrected BDF's linear solve on its own (a test hook): A (row-major,
+ * n x n, n <= 128) x = b.  Returns 1, or 0 on an exactly zero pivot. */
+int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, double* x) {
+  static __thread dmat M;
+  int piv[ORC_MAX_BDF_DIM];
+  double rinv[ORC_MAX_BDF_DIM];
+  if (n < 1 || n > ORC_MAX_BDF_DIM) return 0;
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) M[r][k] = A[r * n + k];
+  if (!corrected_factor(n, M, piv, rinv)) return 0;
+  for (int r = 0; r < n; ++r) x[r] = b[r];
+  corrected_solve(n, M, piv, rinv, x);
+  return 1;
 }

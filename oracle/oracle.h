@@ -150,6 +150,10 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
                              double* t_out, int64_t* accepted, int64_t* rejected,
                              double* traj_t, double* traj_y, int64_t traj_cap);
 
+/* The corrected BDF's linear solve on its own (a test hook): A (row-major,
+ * n x n, n <= 128) x = b.  Returns 1, or 0 on an exactly zero pivot. */
+int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, double* x);
+
 /* ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) -- */
 typedef struct {
   int32_t order;         /* 5 (Adams5) or 3 (Adams3) */

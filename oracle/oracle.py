@@ -106,6 +106,8 @@ def lib():
             L.oracle_bdf_solve_one.argtypes = [
                 ctypes.POINTER(_BdfCfg), ctypes.c_int32, ctypes.c_int32, dp, dp,
                 ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
+            L.oracle_corrected_linsolve.restype = ctypes.c_int
+            L.oracle_corrected_linsolve.argtypes = [ctypes.c_int32, dp, dp, dp]
         if hasattr(L, "oracle_adams_solve_one"):
             L.oracle_rootn.restype = ctypes.c_double
             L.oracle_rootn.argtypes = [ctypes.c_double, ctypes.c_int]
@@ -209,6 +211,16 @@ def rk_solve_batch(cfg, rhs, y0_soa, params_soa, t0, t_end, shared=None, threads
 
 def qrt(x: float) -> float:
     return lib().oracle_qrt(float(x))
+
+
+def corrected_linsolve(A, b):
+    """The corrected BDF's linear solve alone (pivoted LU, row-scaled U,
+    inverted 32x32 diagonal blocks): x with A x = b, or None on a zero pivot."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    ok = lib().oracle_corrected_linsolve(A.shape[0], _dp(A), _dp(b), _dp(x))
+    return x if ok else None
 
 
 def norm(x, dyn_dim=False) -> float:
