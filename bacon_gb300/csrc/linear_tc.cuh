@@ -227,13 +227,22 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
         constexpr uint32_t idesc = tc_idesc();
         unsigned char* sA = tc_smem + buf * kTcBufBytes;
         unsigned char* sB = sA + kTcSlices * kABytes;
-#pragma unroll 1
+        // One descriptor per operand buffer; each MMA's operand is a
+        // compile-time byte offset from it, added to the 14-bit start-address
+        // field (addresses stay below 228 KiB, so the field never carries).
+        // The loops are unrolled: the issuing thread spends a couple of
+        // instructions per MMA, not a descriptor build.
+        const uint64_t a0 = umma_desc(smem_addr(sA), 128, kKg * 128);
+        const uint64_t b0 = umma_desc(smem_addr(sB), 128, kKg * 128);
+#pragma unroll
         for (int ks = 0; ks < kTcKc / 16; ++ks) {
+#pragma unroll
           for (int s = 0; s < kTcSlices; ++s) {
+#pragma unroll
             for (int t = 0; s + t < kTcSlices; ++t) {
               const int d = s + t;
-              const uint64_t ad = umma_desc(smem_addr(sA + s * kABytes + ks * 256), 128, kKg * 128);
-              const uint64_t bd = umma_desc(smem_addr(sB + t * kBBytes + ks * 256), 128, kKg * 128);
+              const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
+              const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
               // The first product into diagonal d is the pair (0, d) of the
               // first K step: it overwrites the accumulator, later ones add.
               const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
