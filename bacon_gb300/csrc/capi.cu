@@ -491,7 +491,12 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   if (tc) {
     BACON_CUDA(c->tc_sa.ensure(static_cast<size_t>(tk.slices) * D * D * sizeof(__nv_bfloat16)));
     BACON_CUDA(c->tc_ea.ensure(D * sizeof(int32_t)));
-    BACON_CUDA(c->tc_sy.ensure(static_cast<size_t>(tk.slices) * n * D * sizeof(__nv_bfloat16)));
+    // the stage-input slices are chunk images of 64-system tiles: padded to
+    // whole tiles, zeroed once (padding systems are never written)
+    const size_t sy_systems = static_cast<size_t>((n + bacon::kTcN - 1) / bacon::kTcN) * bacon::kTcN;
+    const size_t sy_bytes = static_cast<size_t>(tk.slices) * sy_systems * D * sizeof(__nv_bfloat16);
+    BACON_CUDA(c->tc_sy.ensure(sy_bytes));
+    BACON_CUDA(cudaMemsetAsync(c->tc_sy.p, 0, sy_bytes, c->stream));
     BACON_CUDA(c->tc_ey.ensure(n * sizeof(int32_t)));
     BACON_CUDA(cudaFuncSetAttribute(tk.gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, tk.smem_bytes));
     ta.st = st;

@@ -15,9 +15,9 @@
 // applies 2^(e_row + e_sys) and the system's dt, and writes K_i.  Pairs with
 // s + t >= NS are dropped: the relative error of the product is ~2^(-6 NS).
 //
-// CTA tile: 128 rows of A x 64 systems, K = 256 in four chunks of 64 staged
-// in shared memory in the canonical no-swizzle K-major layout (8 x 16-byte
-// core matrices).  One thread issues the MMAs (M128 N64 K16), commits them to
+// CTA tile: 128 rows of A x 64 systems, K = D in chunks of 32 staged in
+// shared memory in the canonical no-swizzle K-major layout (8 x 16-byte core
+// matrices).  One thread issues the MMAs (M128 N64 K16), commits them to
 // an mbarrier, and every wait on it is bounded.
 #pragma once
 
@@ -36,9 +36,9 @@ constexpr int kTcTmemCols = 512;  // kTcSlices accumulators x 64 columns, rounde
 
 struct TcArgs {
   LinArgs st;
-  const __nv_bfloat16* sa;  // [NS][D][D]   slices of A (row r, column k)
+  const __nv_bfloat16* sa;  // slices of A, chunk images (tc_tile_index, 128-row tiles)
   const int32_t* ea;        // [D]          row exponents of A
-  const __nv_bfloat16* sy;  // [NS][n][D]   slices of the stage inputs (system, component)
+  const __nv_bfloat16* sy;  // slices of the stage inputs, chunk images (64-system tiles, padded)
   const int32_t* ey;        // [n]          system exponents
   int stage;
   unsigned int* error_flag; // set when a bounded wait gives up
@@ -117,48 +117,50 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 // --- the stage GEMM ------------------------------------------------------------
 // Persistent: one CTA per SM walks the (64-system, 128-row) tiles.  K = D is
-// staged in chunks of 32 with cp.async into two buffers, each holding the A
-// slices [NS][128 x 32] (8 KiB each) and B slices [NS][64 x 32] (4 KiB each):
-// 2 x 72 KiB.  The chunk after the current one loads while the tensor cores
-// work on the current one; the buffer it overwrites is released by the
-// mbarrier its last MMAs committed to.  Every wait is bounded.
+// staged in chunks of 32 into two buffers, each holding the A slices
+// [NS][128 x 32] (8 KiB each) and B slices [NS][64 x 32] (4 KiB each):
+// 2 x 72 KiB.  The slices are stored in global memory as images of these
+// chunks, so a chunk arrives by two bulk copies (cp.async.bulk, completion
+// counted in bytes on the buffer's full barrier) issued by one thread; with
+// 16-byte cp.async from every thread, issuing the copies took 4.4k cycles per
+// chunk, more than the MMAs.  The chunk after the current one loads while the
+// tensor cores work on the current one; the buffer it overwrites is released
+// by the mbarrier its last MMAs committed to.  Every wait is bounded.
 constexpr int kTcBufBytes = kTcSlices * (kTcM + kTcN) * kTcKc * 2;
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// Issues the cp.async copies of chunk kc of tile (r0, s0) into buffer buf.
+// The slices live in global memory as images of the shared-memory chunks:
+// chunk c of a tile (128 rows of A, or 64 systems) is kTcSlices blocks of
+// (rows x 32) bf16 in the canonical no-swizzle K-major order (8 x 16-byte
+// core matrices, K-adjacent core matrices 128 bytes apart, 8-row groups
+// kTcKc * 16 bytes apart), back to back.  A chunk is then two contiguous
+// copies (A and B parts), issued by one thread.
 template <int D>
-__device__ __forceinline__ void tc_load_chunk(const TcArgs& a, unsigned char* buf, int r0, int64_t s0, int kc,
-                                              int tid) {
-  constexpr int kABytes = kTcM * kTcKc * 2;
-  constexpr int kBBytes = kTcN * kTcKc * 2;
-  constexpr int kKg = kTcKc / 8;  // 16-byte groups along K
-  const int64_t n = a.st.n;
-  unsigned char* sA = buf;
-  unsigned char* sB = buf + kTcSlices * kABytes;
-  for (int v = tid; v < kTcSlices * kTcM * kKg; v += 256) {
-    const int s = v / (kTcM * kKg);
-    const int rem = v % (kTcM * kKg);
-    const int m = rem / kKg, kg = rem % kKg;
-    const __nv_bfloat16* src = a.sa + (static_cast<int64_t>(s) * D + r0 + m) * D + kc + kg * 8;
-    cp_async16(smem_addr(sA + s * kABytes + (m / 8) * (kKg * 128) + kg * 128 + (m % 8) * 16), src, true);
-  }
-  for (int v = tid; v < kTcSlices * kTcN * kKg; v += 256) {
-    const int s = v / (kTcN * kKg);
-    const int rem = v % (kTcN * kKg);
-    const int c = rem / kKg, kg = rem % kKg;
-    const int64_t sys = s0 + c;
-    const bool valid = sys < n;
-    const __nv_bfloat16* src = a.sy + (static_cast<int64_t>(s) * n + (valid ? sys : 0)) * D + kc + kg * 8;
-    cp_async16(smem_addr(sB + s * kBBytes + (c / 8) * (kKg * 128) + kg * 128 + (c % 8) * 16), src, valid);
-  }
-  cp_async_commit();
+__device__ __forceinline__ int64_t tc_tile_index(int rows, int64_t r, int s, int k) {
+  constexpr int kChunks = D / kTcKc;
+  const int64_t tile = r / rows;
+  const int m = static_cast<int>(r - tile * rows);
+  const int c = k / kTcKc, kk = k % kTcKc;
+  const int64_t block = (tile * kChunks + c) * kTcSlices + s;
+  return block * (rows * kTcKc) + (m / 8) * (kTcKc * 8) + (kk / 8) * 64 + (m % 8) * 8 + (kk % 8);
+}
+
+// One thread: announce a chunk's bytes on the buffer's mbarrier and start
+// its two bulk copies (sizes multiples of 16 bytes, addresses 16-byte
+// aligned).
+__device__ __forceinline__ void tc_issue_chunk(uint32_t full_bar, unsigned char* dst, const __nv_bfloat16* srcA,
+                                               const __nv_bfloat16* srcB) {
+  constexpr uint32_t kABytes = kTcSlices * kTcM * kTcKc * 2;
+  constexpr uint32_t kBBytes = kTcSlices * kTcN * kTcKc * 2;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full_bar), "r"(kABytes + kBBytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(srcA), "r"(kABytes), "r"(full_bar)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst + kABytes)),
+               "l"(srcB), "r"(kBBytes), "r"(full_bar)
+               : "memory");
 }
 
 template <int D>
@@ -169,9 +171,11 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
   constexpr int kChunks = D / kTcKc;
   constexpr int kKg = kTcKc / 8;
   static_assert(kChunks >= 2, "two-buffer pipeline needs two chunks");
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t mbar[2];      // the MMAs of the buffer's chunk are done
+  __shared__ __align__(8) uint64_t full_bar[2];  // the buffer's chunk has arrived
   __shared__ uint32_t tmem_base_sh;
   __shared__ int any_running;
+  __shared__ int ok_sh;
 
   const int tid = threadIdx.x;
   const int warp = tid / 32;
@@ -186,15 +190,21 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])) : "memory");
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full_bar[b])) : "memory");
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
-  uint32_t phase[2] = {0u, 0u};
+  // Phases and pending commits, kept by thread 0 (the only thread that waits
+  // on the chunk barriers and issues copies and MMAs).
+  uint32_t phase[2] = {0u, 0u}, fphase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  bool inflight[2] = {false, false};  // copies issued, their arrival not yet waited for
   bool ok = true;
 
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
@@ -206,64 +216,81 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
     __syncthreads();
     if (!any_running) continue;
 
-    tc_load_chunk<D>(a, tc_smem, r0, s0, 0, tid);
-    for (int c = 0; c < kChunks; ++c) {
-      const int buf = c & 1;
-      if (c + 1 < kChunks) {
-        // buffer (c+1)&1 was read by the MMAs of chunk c-1: wait for them
-        if (c >= 1) {
-          if (ok && !mbar_wait_bounded(smem_addr(&mbar[buf ^ 1]), phase[buf ^ 1], a.error_flag)) ok = false;
-          phase[buf ^ 1] ^= 1u;
-        }
-        tc_load_chunk<D>(a, tc_smem + (buf ^ 1) * kTcBufBytes, r0, s0, (c + 1) * kTcKc, tid);
-        cp_async_wait<1>();
-      } else {
-        cp_async_wait<0>();
+    if (tid == 0) {
+      // Thread 0 runs the pipeline: chunk c+1 copies into the other buffer
+      // once the MMAs of chunk c-1 (its last reader) are done, then chunk c's
+      // MMAs are issued when its copies have arrived.  Every wait is bounded;
+      // after a timeout no wait is attempted again.
+      const __nv_bfloat16* srcA = a.sa + static_cast<int64_t>(r0 / kTcM) * kChunks * kTcSlices * (kTcM * kTcKc);
+      const __nv_bfloat16* srcB = a.sy + static_cast<int64_t>(s0 / kTcN) * kChunks * kTcSlices * (kTcN * kTcKc);
+      constexpr int64_t kAChunk = kTcSlices * kTcM * kTcKc, kBChunk = kTcSlices * kTcN * kTcKc;  // elements
+      if (ok) {
+        tc_issue_chunk(smem_addr(&full_bar[0]), tc_smem, srcA, srcB);
+        inflight[0] = true;
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0 && ok) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        constexpr uint32_t idesc = tc_idesc();
-        unsigned char* sA = tc_smem + buf * kTcBufBytes;
-        unsigned char* sB = sA + kTcSlices * kABytes;
-        // One descriptor per operand buffer; each MMA's operand is a
-        // compile-time byte offset from it, added to the 14-bit start-address
-        // field (addresses stay below 228 KiB, so the field never carries).
-        // The loops are unrolled: the issuing thread spends a couple of
-        // instructions per MMA, not a descriptor build.
-        const uint64_t a0 = umma_desc(smem_addr(sA), 128, kKg * 128);
-        const uint64_t b0 = umma_desc(smem_addr(sB), 128, kKg * 128);
-#pragma unroll
-        for (int ks = 0; ks < kTcKc / 16; ++ks) {
-#pragma unroll
-          for (int s = 0; s < kTcSlices; ++s) {
-#pragma unroll
-            for (int t = 0; s + t < kTcSlices; ++t) {
-              const int d = s + t;
-              const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
-              const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
-              // The first product into diagonal d is the pair (0, d) of the
-              // first K step: it overwrites the accumulator, later ones add.
-              const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
-              tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
-            }
+      for (int c = 0; c < kChunks; ++c) {
+        const int buf = c & 1;
+        if (c + 1 < kChunks) {
+          const int nb = buf ^ 1;
+          if (pending[nb]) {
+            if (ok && !mbar_wait_bounded(smem_addr(&mbar[nb]), phase[nb], a.error_flag)) ok = false;
+            phase[nb] ^= 1u;
+            pending[nb] = false;
+          }
+          if (ok) {
+            tc_issue_chunk(smem_addr(&full_bar[nb]), tc_smem + nb * kTcBufBytes, srcA + (c + 1) * kAChunk,
+                           srcB + (c + 1) * kBChunk);
+            inflight[nb] = true;
           }
         }
-        tc_commit(smem_addr(&mbar[buf]));
+        if (ok) {
+          if (mbar_wait_bounded(smem_addr(&full_bar[buf]), fphase[buf], a.error_flag)) inflight[buf] = false;
+          else ok = false;
+          fphase[buf] ^= 1u;
+        }
+        if (ok) {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          constexpr uint32_t idesc = tc_idesc();
+          unsigned char* sA = tc_smem + buf * kTcBufBytes;
+          unsigned char* sB = sA + kTcSlices * kABytes;
+          // One descriptor per operand buffer; each MMA's operand is a
+          // compile-time byte offset from it, added to the 14-bit
+          // start-address field (addresses stay below 228 KiB, so the field
+          // never carries).  The loops are unrolled: a couple of instructions
+          // per MMA, not a descriptor build.
+          const uint64_t a0 = umma_desc(smem_addr(sA), 128, kKg * 128);
+          const uint64_t b0 = umma_desc(smem_addr(sB), 128, kKg * 128);
+#pragma unroll
+          for (int ks = 0; ks < kTcKc / 16; ++ks) {
+#pragma unroll
+            for (int s = 0; s < kTcSlices; ++s) {
+#pragma unroll
+              for (int t = 0; s + t < kTcSlices; ++t) {
+                const int d = s + t;
+                const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
+                const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
+                // The first product into diagonal d is the pair (0, d) of the
+                // first K step: it overwrites the accumulator, later ones add.
+                const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
+                tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+              }
+            }
+          }
+          tc_commit(smem_addr(&mbar[buf]));
+          pending[buf] = true;
+        }
       }
-      __syncthreads();
+      // the MMAs of both buffers' last chunks are done
+      for (int b = 0; b < 2; ++b)
+        if (pending[b]) {
+          if (ok && !mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag)) ok = false;
+          phase[b] ^= 1u;
+          pending[b] = false;
+        }
+      ok_sh = ok ? 1 : 0;
     }
-    // the last chunk's MMAs (and, through them, all earlier ones) are done
-    {
-      // (after a timeout no wait is attempted again: the kernel only frees
-      // its resources and returns)
-      const int last = (kChunks - 1) & 1;
-      if (ok && !mbar_wait_bounded(smem_addr(&mbar[last ^ 1]), phase[last ^ 1], a.error_flag)) ok = false;
-      phase[last ^ 1] ^= 1u;
-      if (ok && !mbar_wait_bounded(smem_addr(&mbar[last]), phase[last], a.error_flag)) ok = false;
-      phase[last] ^= 1u;
-    }
+    __syncthreads();
+    ok = ok_sh != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
       // Epilogue: warps 0..3 own TMEM lanes (rows) 32w..32w+31, warps 4..7
@@ -302,7 +329,11 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  cp_async_wait<0>();
+  // after a timeout: wait (bounded) for copies still in flight into this
+  // CTA's shared memory before it exits
+  if (tid == 0)
+    for (int b = 0; b < 2; ++b)
+      if (inflight[b]) mbar_wait_bounded(smem_addr(&full_bar[b]), fphase[b], a.error_flag);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -378,7 +409,7 @@ __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_
     __nv_bfloat16 qs[kTcSlices];
     tc_slices(v[q], e, qs);
 #pragma unroll
-    for (int s = 0; s < kTcSlices; ++s) sy[(static_cast<int64_t>(s) * n + sys) * D + lane + 32 * q] = qs[s];
+    for (int s = 0; s < kTcSlices; ++s) sy[tc_tile_index<D>(kTcN, sys, s, lane + 32 * q)] = qs[s];
   }
 }
 
@@ -409,7 +440,7 @@ __global__ void __launch_bounds__(256) lin_tc_slice_a_kernel(const double* A, __
     __nv_bfloat16 qs[kTcSlices];
     tc_slices(v[q], e, qs);
 #pragma unroll
-    for (int s = 0; s < kTcSlices; ++s) sa[(static_cast<int64_t>(s) * D + row) * D + lane + 32 * q] = qs[s];
+    for (int s = 0; s < kTcSlices; ++s) sa[tc_tile_index<D>(kTcM, row, s, lane + 32 * q)] = qs[s];
   }
 }
 
