@@ -176,6 +176,9 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
   __shared__ uint32_t tmem_base_sh;
   __shared__ int any_running;
   __shared__ int ok_sh;
+  __shared__ int tile_live[kTcN];          // the tile's systems: running (and < n)
+  __shared__ int tile_ey[kTcN];            // their exponents
+  __shared__ long long tile_dt[kTcN];      // the bits of their dt
 
   const int tid = threadIdx.x;
   const int warp = tid / 32;
@@ -212,7 +215,15 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
     const int64_t s0 = (tile % ntx) * kTcN;
     if (tid == 0) any_running = 0;
     __syncthreads();
-    if (tid < kTcN && s0 + tid < n && a.st.status[s0 + tid] == kLinRunning) any_running = 1;
+    if (tid < kTcN) {
+      // the epilogue's per-system data, read once per tile
+      const int64_t sys = s0 + tid;
+      const bool live = sys < n && a.st.status[sys] == kLinRunning;
+      tile_live[tid] = live ? 1 : 0;
+      tile_ey[tid] = live ? a.ey[sys] : 0;
+      tile_dt[tid] = live ? __double_as_longlong(a.st.dt[sys]) : 0ll;
+      if (live) any_running = 1;
+    }
     __syncthreads();
     if (!any_running) continue;
 
@@ -315,12 +326,25 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
         }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
+          if (!tile_live[cb + j]) continue;
           const int64_t sys = s0 + cb + j;
-          if (sys >= n || a.st.status[sys] != kLinRunning) continue;
-          const int pe = erow + a.ey[sys] - kTcBits * (kTcSlices + 1);
-          const double p2 = (pe >= -1022 && pe <= 1023) ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
-                                                       : ldexp(1.0, pe);
-          a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = (__ll2double_rn(acc[j]) * p2) * a.st.dt[sys];
+          const int pe = erow + tile_ey[cb + j] - kTcBits * (kTcSlices + 1);
+          const long long dtb = tile_dt[cb + j];
+          const int dte = static_cast<int>((dtb >> 52) & 0x7ff);
+          const double x = __ll2double_rn(acc[j]);
+          double k;
+          if (dte != 0 && dte != 0x7ff && dte + pe >= 1 && dte + pe <= 2046) {
+            // (x 2^pe) dt = x (2^pe dt): the power-of-two scaling of dt stays
+            // normal, so it is exact, and it is done on the exponent field
+            // (one product per element instead of two)
+            k = x * __longlong_as_double(dtb + static_cast<long long>(pe) * (1ll << 52));
+          } else {
+            const double p2 = (pe >= -1022 && pe <= 1023)
+                                  ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
+                                  : ldexp(1.0, pe);
+            k = (x * p2) * __longlong_as_double(dtb);
+          }
+          a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = k;
         }
       }
     }
