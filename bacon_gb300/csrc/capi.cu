@@ -527,7 +527,8 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
         void* slargs[] = {&ta, &sy, &ey};
         BACON_CUDA(cudaLaunchKernel(tk.slice[s], dim3(cg), dim3(256), slargs, 0, c->stream));
         void* gargs[] = {&ta};
-        BACON_CUDA(cudaLaunchKernel(tk.gemm, tg, dim3(256), gargs, static_cast<size_t>(tk.smem_bytes), c->stream));
+        BACON_CUDA(cudaLaunchKernel(tk.gemm, tg, dim3(static_cast<unsigned>(tk.gemm_threads)), gargs,
+                                    static_cast<size_t>(tk.smem_bytes), c->stream));
         c->launches += 1;
       } else {
         BACON_CUDA(cudaLaunchKernel(k.stage[s], sg, dim3(256), sargs, 0, c->stream));

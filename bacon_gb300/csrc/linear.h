@@ -26,6 +26,7 @@ struct LinTcKernels {
   const void* slice[6] = {};       // __global__ void(TcArgs, bf16* sy, int32_t* ey)
   const void* gemm = nullptr;      // __global__ void(TcArgs)
   int smem_bytes = 0;
+  int gemm_threads = 0;
   int slices = 0;
 };
 bool lin_tc_kernels(int method, int layout, int dim, LinTcKernels& k);

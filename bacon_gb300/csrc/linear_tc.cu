@@ -21,6 +21,7 @@ void fill_tc(LinTcKernels& k) {
   }
   k.gemm = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D>);
   k.smem_bytes = 2 * kTcBufBytes;
+  k.gemm_threads = kTcThreads;
   k.slices = kTcSlices;
 }
 

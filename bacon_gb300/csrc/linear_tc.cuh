@@ -17,8 +17,10 @@
 //
 // CTA tile: 128 rows of A x 64 systems, K = D in chunks of 32 staged in
 // shared memory in the canonical no-swizzle K-major layout (8 x 16-byte core
-// matrices).  One thread issues the MMAs (M128 N64 K16), commits them to
-// an mbarrier, and every wait on it is bounded.
+// matrices).  One producer thread issues the copies and the MMAs (M128 N64
+// K16) and commits them to mbarriers; eight epilogue warps drain the
+// accumulators, so a tile's epilogue overlaps the next tile's MMAs.  Every
+// wait on an mbarrier is bounded.
 #pragma once
 
 #include <cstdint>
@@ -163,18 +165,38 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t full_bar, unsigned char*
                : "memory");
 }
 
+// Warp roles.  Warps 0..7 run the epilogue: warp w reads TMEM lanes
+// 32(w%4)..32(w%4)+31 (the rows of its quadrant) for half of the tile's 64
+// columns.  Warp 8 is the producer: its lane 0 issues the copies and the MMAs.
+// The accumulators are handed over through two mbarriers: tmem_full (the
+// tile's last MMAs are done, by tcgen05.commit) and tmem_empty (the epilogue
+// warps have read every diagonal into registers).  The FP64 conversion,
+// scaling and stores of tile j then run while the MMAs of tile j+1 fill TMEM.
+constexpr int kTcEpiWarps = 8;
+constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);
+
+__device__ __forceinline__ void tc_epi_sync() {  // named barrier 1: the epilogue warps only
+  asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcEpiWarps) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
 template <int D>
-__global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   constexpr int kABytes = kTcM * kTcKc * 2;  // 8192
   constexpr int kBBytes = kTcN * kTcKc * 2;  // 4096
   constexpr int kChunks = D / kTcKc;
   constexpr int kKg = kTcKc / 8;
-  static_assert(kChunks >= 2, "two-buffer pipeline needs two chunks");
+  static_assert(kChunks >= 2 && kChunks % 2 == 0, "every tile starts in buffer 0 of the two-buffer pipeline");
   __shared__ __align__(8) uint64_t mbar[2];      // the MMAs of the buffer's chunk are done
   __shared__ __align__(8) uint64_t full_bar[2];  // the buffer's chunk has arrived
+  __shared__ __align__(8) uint64_t tmem_full;    // the tile's accumulators are complete
+  __shared__ __align__(8) uint64_t tmem_empty;   // the epilogue has read them
   __shared__ uint32_t tmem_base_sh;
-  __shared__ int any_running;
+  __shared__ int any_w[2];
   __shared__ int ok_sh;
   __shared__ int tile_live[kTcN];          // the tile's systems: running (and < n)
   __shared__ int tile_ey[kTcN];            // their exponents
@@ -182,6 +204,7 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
 
   const int tid = threadIdx.x;
   const int warp = tid / 32;
+  const int lane = tid % 32;
   const int64_t n = a.st.n;
   const int64_t ntx = (n + kTcN - 1) / kTcN;
   const int64_t ntiles = ntx * (D / kTcM);
@@ -197,167 +220,188 @@ __global__ void __launch_bounds__(256, 1) lin_tc_stage_kernel(const TcArgs a) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[b])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full_bar[b])) : "memory");
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tmem_full)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tmem_empty)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
-  // Phases and pending commits, kept by thread 0 (the only thread that waits
-  // on the chunk barriers and issues copies and MMAs).
-  uint32_t phase[2] = {0u, 0u}, fphase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
-  bool inflight[2] = {false, false};  // copies issued, their arrival not yet waited for
-  bool ok = true;
 
-  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int r0 = static_cast<int>(tile / ntx) * kTcM;
-    const int64_t s0 = (tile % ntx) * kTcN;
-    if (tid == 0) any_running = 0;
-    __syncthreads();
-    if (tid < kTcN) {
-      // the epilogue's per-system data, read once per tile
-      const int64_t sys = s0 + tid;
-      const bool live = sys < n && a.st.status[sys] == kLinRunning;
-      tile_live[tid] = live ? 1 : 0;
-      tile_ey[tid] = live ? a.ey[sys] : 0;
-      tile_dt[tid] = live ? __double_as_longlong(a.st.dt[sys]) : 0ll;
-      if (live) any_running = 1;
-    }
-    __syncthreads();
-    if (!any_running) continue;
-
-    if (tid == 0) {
-      // Thread 0 runs the pipeline: chunk c+1 copies into the other buffer
-      // once the MMAs of chunk c-1 (its last reader) are done, then chunk c's
-      // MMAs are issued when its copies have arrived.  Every wait is bounded;
-      // after a timeout no wait is attempted again.
-      const __nv_bfloat16* srcA = a.sa + static_cast<int64_t>(r0 / kTcM) * kChunks * kTcSlices * (kTcM * kTcKc);
-      const __nv_bfloat16* srcB = a.sy + static_cast<int64_t>(s0 / kTcN) * kChunks * kTcSlices * (kTcN * kTcKc);
-      constexpr int64_t kAChunk = kTcSlices * kTcM * kTcKc, kBChunk = kTcSlices * kTcN * kTcKc;  // elements
-      if (ok) {
-        tc_issue_chunk(smem_addr(&full_bar[0]), tc_smem, srcA, srcB);
-        inflight[0] = true;
-      }
-      for (int c = 0; c < kChunks; ++c) {
-        const int buf = c & 1;
-        if (c + 1 < kChunks) {
-          const int nb = buf ^ 1;
-          if (pending[nb]) {
-            if (ok && !mbar_wait_bounded(smem_addr(&mbar[nb]), phase[nb], a.error_flag)) ok = false;
-            phase[nb] ^= 1u;
-            pending[nb] = false;
+  if (warp == kTcEpiWarps) {
+    // ---- producer ----------------------------------------------------------
+    // Both roles walk the same tiles and skip the same ones (a tile whose 64
+    // systems have all stopped); status is not written during the launch.
+    // Lane 0 runs the pipeline: chunk c+1 copies into the other buffer once
+    // the MMAs of its last reader are done, chunk c's MMAs are issued when
+    // its copies have arrived, and a tile's first MMAs wait until the
+    // epilogue has read the previous tile's accumulators.  Every wait is
+    // bounded; after a timeout no wait is attempted again until the drain.
+    uint32_t phase[2] = {0u, 0u}, fphase[2] = {0u, 0u}, ephase = 0u;
+    bool pending[2] = {false, false};   // MMAs committed to mbar[b], not yet waited for
+    bool inflight[2] = {false, false};  // copies issued, their arrival not yet waited for
+    bool ok = true, first = true;
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int r0 = static_cast<int>(tile / ntx) * kTcM;
+      const int64_t s0 = (tile % ntx) * kTcN;
+      const int64_t sa0 = s0 + lane, sa1 = s0 + 32 + lane;
+      const bool live = (sa0 < n && a.st.status[sa0] == kLinRunning) || (sa1 < n && a.st.status[sa1] == kLinRunning);
+      if (!__any_sync(0xffffffffu, live)) continue;
+      if (lane == 0) {
+        const __nv_bfloat16* srcA = a.sa + static_cast<int64_t>(r0 / kTcM) * kChunks * kTcSlices * (kTcM * kTcKc);
+        const __nv_bfloat16* srcB = a.sy + static_cast<int64_t>(s0 / kTcN) * kChunks * kTcSlices * (kTcN * kTcKc);
+        constexpr int64_t kAChunk = kTcSlices * kTcM * kTcKc, kBChunk = kTcSlices * kTcN * kTcKc;  // elements
+        auto load = [&](int b, int c) {
+          if (pending[b]) {
+            if (ok && !mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag)) ok = false;
+            phase[b] ^= 1u;
+            pending[b] = false;
           }
           if (ok) {
-            tc_issue_chunk(smem_addr(&full_bar[nb]), tc_smem + nb * kTcBufBytes, srcA + (c + 1) * kAChunk,
-                           srcB + (c + 1) * kBChunk);
-            inflight[nb] = true;
+            tc_issue_chunk(smem_addr(&full_bar[b]), tc_smem + b * kTcBufBytes, srcA + c * kAChunk, srcB + c * kBChunk);
+            inflight[b] = true;
           }
-        }
-        if (ok) {
-          if (mbar_wait_bounded(smem_addr(&full_bar[buf]), fphase[buf], a.error_flag)) inflight[buf] = false;
-          else ok = false;
-          fphase[buf] ^= 1u;
-        }
-        if (ok) {
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          constexpr uint32_t idesc = tc_idesc();
-          unsigned char* sA = tc_smem + buf * kTcBufBytes;
-          unsigned char* sB = sA + kTcSlices * kABytes;
-          // One descriptor per operand buffer; each MMA's operand is a
-          // compile-time byte offset from it, added to the 14-bit
-          // start-address field (addresses stay below 228 KiB, so the field
-          // never carries).  The loops are unrolled: a couple of instructions
-          // per MMA, not a descriptor build.
-          const uint64_t a0 = umma_desc(smem_addr(sA), 128, kKg * 128);
-          const uint64_t b0 = umma_desc(smem_addr(sB), 128, kKg * 128);
+        };
+        load(0, 0);
+        // unrolled, so the buffer index and the per-buffer phases are
+        // compile-time (registers, not a stack frame)
 #pragma unroll
-          for (int ks = 0; ks < kTcKc / 16; ++ks) {
+        for (int c = 0; c < kChunks; ++c) {
+          const int buf = c & 1;
+          if (c + 1 < kChunks) load(buf ^ 1, c + 1);
+          if (ok) {
+            if (mbar_wait_bounded(smem_addr(&full_bar[buf]), fphase[buf], a.error_flag)) inflight[buf] = false;
+            else ok = false;
+            fphase[buf] ^= 1u;
+          }
+          if (ok && c == 0 && !first) {
+            if (!mbar_wait_bounded(smem_addr(&tmem_empty), ephase, a.error_flag)) ok = false;
+            ephase ^= 1u;
+          }
+          if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            constexpr uint32_t idesc = tc_idesc();
+            unsigned char* sA = tc_smem + buf * kTcBufBytes;
+            unsigned char* sB = sA + kTcSlices * kABytes;
+            // One descriptor per operand buffer; each MMA's operand is a
+            // compile-time byte offset from it, added to the 14-bit
+            // start-address field (addresses stay below 228 KiB, so the
+            // field never carries).
+            const uint64_t a0 = umma_desc(smem_addr(sA), 128, kKg * 128);
+            const uint64_t b0 = umma_desc(smem_addr(sB), 128, kKg * 128);
 #pragma unroll
-            for (int s = 0; s < kTcSlices; ++s) {
+            for (int ks = 0; ks < kTcKc / 16; ++ks) {
 #pragma unroll
-              for (int t = 0; s + t < kTcSlices; ++t) {
-                const int d = s + t;
-                const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
-                const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
-                // The first product into diagonal d is the pair (0, d) of the
-                // first K step: it overwrites the accumulator, later ones add.
-                const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
-                tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+              for (int s = 0; s < kTcSlices; ++s) {
+#pragma unroll
+                for (int t = 0; s + t < kTcSlices; ++t) {
+                  const int d = s + t;
+                  const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
+                  const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
+                  // The first product into diagonal d is the pair (0, d) of
+                  // the first K step: it overwrites the accumulator.
+                  const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
+                  tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+                }
               }
             }
+            tc_commit(smem_addr(&mbar[buf]));
+            pending[buf] = true;
+            if (c + 1 == kChunks) tc_commit(smem_addr(&tmem_full));
           }
-          tc_commit(smem_addr(&mbar[buf]));
-          pending[buf] = true;
         }
       }
-      // the MMAs of both buffers' last chunks are done
-      for (int b = 0; b < 2; ++b)
-        if (pending[b]) {
-          if (ok && !mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag)) ok = false;
-          phase[b] ^= 1u;
-          pending[b] = false;
-        }
-      ok_sh = ok ? 1 : 0;
+      first = false;
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     }
-    __syncthreads();
-    ok = ok_sh != 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-      // Epilogue: warps 0..3 own TMEM lanes (rows) 32w..32w+31, warps 4..7
-      // the same rows for the second half of the 64 columns.
-      const int rw = warp % 4;
-      const int row = r0 + rw * 32 + (tid % 32);
-      const int cbase = (warp / 4) * 32;
-      const int erow = a.ea[row];
-      for (int cb = cbase; cb < cbase + 32; cb += 16) {
-        // Diagonal d holds an exact integer below 2^23 scaled by 2^(-6(d+2)):
-        // the sum over d is an exact 64-bit integer times 2^-42.
-        long long acc[16];
+    if (lane == 0) {
+      // drain (bounded): the MMAs and the copies still in flight into this
+      // CTA's shared memory and tensor memory
 #pragma unroll
-        for (int j = 0; j < 16; ++j) acc[j] = 0;
+      for (int b = 0; b < 2; ++b)
+        if (pending[b]) mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag);
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+        if (inflight[b]) mbar_wait_bounded(smem_addr(&full_bar[b]), fphase[b], a.error_flag);
+    }
+  } else {
+    // ---- epilogue ----------------------------------------------------------
+    // Warps 0..3 own TMEM lanes (rows) 32w..32w+31 for columns 0..31, warps
+    // 4..7 the same rows for columns 32..63.  Every decision that ends or
+    // skips an iteration is read from shared memory after a barrier of all
+    // 256 epilogue threads, so they all take the same path.
+    const int rw = warp % 4;
+    const int cbase = (warp / 4) * 32;
+    uint32_t tphase = 0u;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+      const int r0 = static_cast<int>(tile / ntx) * kTcM;
+      const int64_t s0 = (tile % ntx) * kTcN;
+      tc_epi_sync();  // the previous tile's readers of tile_* are done
+      if (tid < kTcN) {
+        // the epilogue's per-system data, read once per tile
+        const int64_t sys = s0 + tid;
+        const bool live = sys < n && a.st.status[sys] == kLinRunning;
+        tile_live[tid] = live ? 1 : 0;
+        tile_ey[tid] = live ? a.ey[sys] : 0;
+        tile_dt[tid] = live ? __double_as_longlong(a.st.dt[sys]) : 0ll;
+        const bool any = __any_sync(0xffffffffu, live);
+        if (lane == 0) any_w[warp] = any ? 1 : 0;
+      }
+      tc_epi_sync();
+      if (!(any_w[0] | any_w[1])) continue;  // the producer skips it too
+      if (tid == 0) ok_sh = mbar_wait_bounded(smem_addr(&tmem_full), tphase, a.error_flag) ? 1 : 0;
+      tc_epi_sync();
+      tphase ^= 1u;
+      if (!ok_sh) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // Diagonal d holds an exact integer below 2^23 scaled by 2^(-6(d+2)):
+      // the sum over d is an exact 64-bit integer times 2^-42.
+      long long acc[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[j] = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
 #pragma unroll
         for (int d = 0; d < kTcSlices; ++d) {
           float v[16];
-          tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cb), v);
+          tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cbase + 16 * h), v);
 #pragma unroll
           for (int j = 0; j < 16; ++j)
-            acc[j] += static_cast<long long>(__float2int_rz(v[j])) << (kTcBits * (kTcSlices - 1 - d));
-        }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          if (!tile_live[cb + j]) continue;
-          const int64_t sys = s0 + cb + j;
-          const int pe = erow + tile_ey[cb + j] - kTcBits * (kTcSlices + 1);
-          const long long dtb = tile_dt[cb + j];
-          const int dte = static_cast<int>((dtb >> 52) & 0x7ff);
-          const double x = __ll2double_rn(acc[j]);
-          double k;
-          if (dte != 0 && dte != 0x7ff && dte + pe >= 1 && dte + pe <= 2046) {
-            // (x 2^pe) dt = x (2^pe dt): the power-of-two scaling of dt stays
-            // normal, so it is exact, and it is done on the exponent field
-            // (one product per element instead of two)
-            k = x * __longlong_as_double(dtb + static_cast<long long>(pe) * (1ll << 52));
-          } else {
-            const double p2 = (pe >= -1022 && pe <= 1023)
-                                  ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
-                                  : ldexp(1.0, pe);
-            k = (x * p2) * __longlong_as_double(dtb);
-          }
-          a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = k;
+            acc[16 * h + j] += static_cast<long long>(__float2int_rz(v[j])) << (kTcBits * (kTcSlices - 1 - d));
         }
       }
+      // hand the accumulators back to the producer
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      tc_epi_sync();
+      if (tid == 0) mbar_arrive(smem_addr(&tmem_empty));
+      const int row = r0 + rw * 32 + lane;
+      const int erow = a.ea[row];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int col = cbase + j;
+        if (!tile_live[col]) continue;
+        const int64_t sys = s0 + col;
+        const int pe = erow + tile_ey[col] - kTcBits * (kTcSlices + 1);
+        const long long dtb = tile_dt[col];
+        const int dte = static_cast<int>((dtb >> 52) & 0x7ff);
+        const double x = __ll2double_rn(acc[j]);
+        double k;
+        if (dte != 0 && dte != 0x7ff && dte + pe >= 1 && dte + pe <= 2046) {
+          // (x 2^pe) dt = x (2^pe dt): the power-of-two scaling of dt stays
+          // normal, so it is exact, and it is done on the exponent field
+          // (one product per element instead of two)
+          k = x * __longlong_as_double(dtb + static_cast<long long>(pe) * (1ll << 52));
+        } else {
+          const double p2 = (pe >= -1022 && pe <= 1023)
+                                ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
+                                : ldexp(1.0, pe);
+          k = (x * p2) * __longlong_as_double(dtb);
+        }
+        a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = k;
+      }
     }
-    // TMEM is overwritten by the next tile's first MMA
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  // after a timeout: wait (bounded) for copies still in flight into this
-  // CTA's shared memory before it exits
-  if (tid == 0)
-    for (int b = 0; b < 2; ++b)
-      if (inflight[b]) mbar_wait_bounded(smem_addr(&full_bar[b]), fphase[b], a.error_flag);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
