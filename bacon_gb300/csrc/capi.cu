@@ -418,7 +418,9 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   const bool tc = opt->precision == BACON_TC_SPLIT;
   bacon::LinKernels k;
   bacon::LinTcKernels tk;
-  if (!bacon::lin_kernels(opt->method, opt->layout, tc ? 0 : opt->precision, p->dim, k) ||
+  // The tensor-core mode takes the FMA engine's control kernel: its stage
+  // values carry ~2^-36 relative error, far above a contraction's rounding.
+  if (!bacon::lin_kernels(opt->method, opt->layout, tc ? 1 : opt->precision, p->dim, k) ||
       (tc && !bacon::lin_tc_kernels(opt->method, opt->layout, p->dim, tk)))
     return fail(BACON_UNSUPPORTED, "linear engine: dim 64/128/256 (128/256 on tensor cores); layouts "
                                    "as_written / fehlberg; precision FP64_EXACT, FP64_FMA or TC_SPLIT");
@@ -479,9 +481,10 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   void* cargs[] = {&st, &first};
   void* sargs[] = {&st};
   const unsigned cg = static_cast<unsigned>((n * 32 + 255) / 256);
+  const unsigned ctl_g = static_cast<unsigned>((n + bacon::kLinCtlSystemsPerBlock - 1) / bacon::kLinCtlSystemsPerBlock);
   const dim3 sg(static_cast<unsigned>((n + 63) / 64), static_cast<unsigned>(D / 64));
   BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
-  BACON_CUDA(cudaLaunchKernel(k.control, dim3(cg), dim3(256), cargs, 0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(k.control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
   BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
   BACON_CUDA(cudaStreamSynchronize(c->stream));
   c->launches += 2;
@@ -535,7 +538,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
       }
     }
     BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
-    BACON_CUDA(cudaLaunchKernel(k.control, dim3(cg), dim3(256), cargs, 0, c->stream));
+    BACON_CUDA(cudaLaunchKernel(k.control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
     BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     if (tc)  // a tensor-core stage that gave up a bounded wait ends the solve
       BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 3, c->d_ctl + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,

@@ -118,62 +118,87 @@ __global__ void __launch_bounds__(256) lin_stage_kernel(const LinArgs a) {
   }
 }
 
-// nalgebra norm of a dim >= 5 vector held by one warp: eight accumulators
-// over strides of 8 (blas.rs dotx), combined in its order.  Lanes 0..7 own
-// the accumulators; the result is valid in every lane.
-template <int D>
-__device__ __forceinline__ double warp_nalgebra_norm(const double* v, unsigned lane) {
-  static_assert(D >= 8 && D % 8 == 0, "dimension must be a multiple of 8");
-  double accl = 0.0;
-  if (lane < 8)
-    for (int i = 0; i < D; i += 8) accl = __dadd_rn(accl, __dmul_rn(v[i + lane], v[i + lane]));
-  double acc[8];
-#pragma unroll
-  for (int l = 0; l < 8; ++l) acc[l] = __shfl_sync(0xffffffffu, accl, l);
-  double res = 0.0;
-  res = __dadd_rn(res, __dadd_rn(acc[0], acc[4]));
-  res = __dadd_rn(res, __dadd_rn(acc[1], acc[5]));
-  res = __dadd_rn(res, __dadd_rn(acc[2], acc[6]));
-  res = __dadd_rn(res, __dadd_rn(acc[3], acc[7]));
-  return __dsqrt_rn(__dadd_rn(0.0, res));
-}
+// Control kernel: finish the attempt in flight (error estimate, accept,
+// controller, dt_min check: rk.rs:386-416), then open the next one (Done /
+// attempt cap, end clamp: rk.rs:362-368).
+//
+// A warp serves kLinCtlGroup = 4 consecutive systems.  The element-wise
+// work (error vector, update of y) runs as full-warp passes over one system
+// at a time.  The nalgebra norm and the scalar controller run once for all
+// four: lanes 8g..8g+7 hold system g's eight norm accumulators (blas.rs
+// dotx: strides of 8, combined in its order) and compute its controller.  On
+// GB300 an FP64 warp instruction costs the same whatever its active lanes,
+// and this kernel is FP64-pipe bound, so the norm with 8 of 32 lanes active
+// and the one-lane controller had cost as much as the vector work.
+constexpr int kLinCtlGroup = 4;    // systems per warp
+constexpr int kLinCtlThreads = 128;
+constexpr int kLinCtlSystemsPerBlock = kLinCtlGroup * kLinCtlThreads / 32;
 
-// Control kernel, one warp per system: finish the attempt in flight (error
-// estimate, accept, controller, dt_min check: rk.rs:386-416), then open the
-// next one (Done / attempt cap, end clamp: rk.rs:362-368).
 template <class Ops, class Tab, int D>
-__global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int first) {
+__global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinArgs a, int first) {
+  static_assert(D >= 8 && D % 32 == 0, "dimension must be a multiple of 32");
   constexpr int S = Tab::S;
   constexpr int PER = D / 32;
+  constexpr int G = kLinCtlGroup;
+  static_assert(G == 4, "the warp-level skip below names four systems");
   const unsigned lane = threadIdx.x & 31u;
-  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
-  if (sys >= a.n) return;
-  if (a.status[sys] != kLinRunning) return;
+  const int w = threadIdx.x / 32;
+  const int g = static_cast<int>(lane / 8);  // this lane's system in the norm and the controller
+  const int r = static_cast<int>(lane % 8);  // its accumulator
   const int64_t n = a.n;
-  double t = a.t[sys], dt = a.dt[sys];
-  const double end = a.end[sys];
-  auto att = a.attempts[sys];
+  const int64_t sys0 = (static_cast<int64_t>(blockIdx.x) * kLinCtlThreads + threadIdx.x) / 32 * G;
+  if (sys0 >= n) return;  // whole warp
+  bool run[G];
+#pragma unroll
+  for (int k = 0; k < G; ++k) run[k] = sys0 + k < n && a.status[sys0 + k] == kLinRunning;
+  if (!(run[0] || run[1] || run[2] || run[3])) return;  // whole warp
+  const int64_t sys = sys0 + g;
+  const bool mine = g == 0 ? run[0] : g == 1 ? run[1] : g == 2 ? run[2] : run[3];  // no stack frame
+  double t = 0.0, dt = 0.0, end = 0.0;
+  int64_t att = 0;
+  if (mine) {
+    t = a.t[sys];
+    dt = a.dt[sys];
+    end = a.end[sys];
+    att = a.attempts[sys];
+  }
   int32_t st = kLinRunning;
+  int32_t acc_add = 0, rej_add = 0;
 
   if (!first) {
-    __shared__ double ev_s[8][D];
-    double* ev = ev_s[threadIdx.x / 32];
-    double yv[PER];
+    __shared__ double ev_s[kLinCtlThreads / 32][G][D];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int d = lane + 32 * q;
-      const int64_t off = sys * D + d;
-      double e = 0.0;
-      if constexpr (Tab::e(0) != 0.0) e = Ops::mul(a.K[off], Tab::e(0));
-      static_for<1, S>([&](auto jc) {
-        constexpr int j = decltype(jc)::value;
-        if constexpr (Tab::e(j) != 0.0) e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::e(j));
-      });
-      ev[d] = e;
-      yv[q] = a.y[off];
+    for (int k = 0; k < G; ++k) {
+      if (!run[k]) continue;  // whole warp
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int d = lane + 32 * q;
+        const int64_t off = (sys0 + k) * D + d;
+        double e = 0.0;
+        if constexpr (Tab::e(0) != 0.0) e = Ops::mul(a.K[off], Tab::e(0));
+        static_for<1, S>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          if constexpr (Tab::e(j) != 0.0) e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::e(j));
+        });
+        ev_s[w][k][d] = e;
+      }
     }
     __syncwarp();
-    const double err = Ops::div(warp_nalgebra_norm<D>(ev, lane), dt);
+    // nalgebra norm of system g's error vector; lanes of a stopped system
+    // compute on stale values and their result is not used
+    const double* ev = ev_s[w][g];
+    double accl = 0.0;
+#pragma unroll 8
+    for (int i = 0; i < D; i += 8) accl = __dadd_rn(accl, __dmul_rn(ev[i + r], ev[i + r]));
+    double acc[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) acc[l] = __shfl_sync(0xffffffffu, accl, 8 * g + l);
+    double res = 0.0;
+    res = __dadd_rn(res, __dadd_rn(acc[0], acc[4]));
+    res = __dadd_rn(res, __dadd_rn(acc[1], acc[5]));
+    res = __dadd_rn(res, __dadd_rn(acc[2], acc[6]));
+    res = __dadd_rn(res, __dadd_rn(acc[3], acc[7]));
+    const double err = Ops::div(__dsqrt_rn(__dadd_rn(0.0, res)), dt);
     const bool ok = err <= a.tol;
     const double tn = ok ? Ops::add(t, dt) : t;
     const double delta = qrt(Ops::div(a.tol, err));
@@ -182,32 +207,39 @@ __global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int f
     else if (delta >= 4.0) ndt = Ops::mul(dt, 4.0);
     else ndt = Ops::mul(dt, delta);
     if (ndt > a.dt_max) ndt = a.dt_max;
+    bool upd = false;
     if (ndt < a.dt_min && tn < end) {
       st = kStMinDt;
     } else if (ok) {
+      upd = true;
+      t = tn;
+      acc_add = 1;
+    } else {
+      rej_add = 1;
+      // dt bitwise unchanged by a rejection: the next attempt is this one
+      // again, up to the cap (as in rk_persistent_kernel); jump there.
+      if (ndt == dt) {
+        rej_add += static_cast<int32_t>(a.max_attempts - att);
+        att = a.max_attempts;
+      }
+    }
+    dt = ndt;
+    // y += sum_j b_j K_j for the accepted systems, a full-warp pass each
+    const unsigned upd_mask = __ballot_sync(0xffffffffu, upd && mine);
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if (!((upd_mask >> (8 * k)) & 1u)) continue;  // whole warp
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
-        const int d = lane + 32 * q;
-        const int64_t off = sys * D + d;
-        double v = yv[q];
+        const int64_t off = (sys0 + k) * D + lane + 32 * q;
+        double v = a.y[off];
         static_for<0, S>([&](auto jc) {
           constexpr int j = decltype(jc)::value;
           if constexpr (Tab::b(j) != 0.0) v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::b(j));
         });
         a.y[off] = v;
       }
-      t = tn;
-      if (lane == 0) a.accepted[sys] += 1;
-    } else {
-      if (lane == 0) a.rejected[sys] += 1;
-      // dt bitwise unchanged by a rejection: the next attempt is this one
-      // again, up to the cap (as in rk_persistent_kernel); jump there.
-      if (ndt == dt) {
-        if (lane == 0) a.rejected[sys] += static_cast<int32_t>(a.max_attempts - att);
-        att = a.max_attempts;
-      }
     }
-    dt = ndt;
   }
   if (st == kLinRunning) {
     if (t >= end) {
@@ -218,7 +250,9 @@ __global__ void __launch_bounds__(256) lin_control_kernel(const LinArgs a, int f
       if (Ops::add(t, dt) >= end) dt = Ops::sub(end, t);
     }
   }
-  if (lane == 0) {
+  if (mine && r == 0) {
+    if (acc_add) a.accepted[sys] += acc_add;
+    if (rej_add) a.rejected[sys] += rej_add;
     a.t[sys] = t;
     a.dt[sys] = dt;
     if (st != kLinRunning) {

@@ -443,26 +443,58 @@ __device__ __forceinline__ unsigned long long tc_abs_bits(double x) {
 }
 
 // Slices of the stage inputs Y_i = y + sum_j M(i,j) K_j, one warp per system.
+// Lane l owns the PER = D/32 consecutive elements from PER*l: it loads them
+// as 16-byte vectors and writes each slice's PER bf16 values with one store
+// (16 bytes for D = 256, 8 for D = 128), since in a chunk image the K index
+// is contiguous in runs of 8.
+template <int PER>
+struct TcSliceVec;
+template <>
+struct TcSliceVec<8> {
+  using T = uint4;
+};
+template <>
+struct TcSliceVec<4> {
+  using T = uint2;
+};
+
+template <int PER>
+__device__ __forceinline__ void tc_load_run(const double* p, double (&v)[PER]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < PER / 2; ++i) {
+    const double2 x = q[i];
+    v[2 * i] = x.x;
+    v[2 * i + 1] = x.y;
+  }
+}
+
 template <class Tab, int D, int STAGE>
 __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_bfloat16* sy, int32_t* ey) {
   constexpr int PER = D / 32;
+  static_assert(PER == 4 || PER == 8, "vector stores of 8 or 16 bytes");
+  using Vec = typename TcSliceVec<PER>::T;
   const unsigned lane = threadIdx.x & 31u;
   const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
   const int64_t n = a.st.n;
   if (sys >= n || a.st.status[sys] != kLinRunning) return;
+  const int64_t off = sys * D + PER * lane;
   double v[PER];
+  tc_load_run<PER>(a.st.y + off, v);
+  static_for<0, Tab::S>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    constexpr double m = Tab::M(STAGE, j);
+    if constexpr (m != 0.0) {
+      double kv[PER];
+      tc_load_run<PER>(a.st.K + (static_cast<int64_t>(j) * n) * D + off, kv);
+#pragma unroll
+      for (int i = 0; i < PER; ++i) v[i] = fma(kv[i], m, v[i]);
+    }
+  });
   unsigned long long mx = 0ull;
 #pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int64_t off = sys * D + lane + 32 * q;
-    double x = a.st.y[off];
-    static_for<0, Tab::S>([&](auto jc) {
-      constexpr int j = decltype(jc)::value;
-      constexpr double m = Tab::M(STAGE, j);
-      if constexpr (m != 0.0) x = fma(a.st.K[(static_cast<int64_t>(j) * n) * D + off], m, x);
-    });
-    v[q] = x;
-    const unsigned long long ab = tc_abs_bits(x);
+  for (int i = 0; i < PER; ++i) {
+    const unsigned long long ab = tc_abs_bits(v[i]);
     mx = ab > mx ? ab : mx;
   }
 #pragma unroll
@@ -472,12 +504,18 @@ __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_
   }
   const int e = tc_exponent_of(mx);
   if (lane == 0) ey[sys] = e;
+  __nv_bfloat16 qs[PER][kTcSlices];
 #pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    __nv_bfloat16 qs[kTcSlices];
-    tc_slices(v[q], e, qs);
+  for (int i = 0; i < PER; ++i) tc_slices(v[i], e, qs[i]);
 #pragma unroll
-    for (int s = 0; s < kTcSlices; ++s) sy[tc_tile_index<D>(kTcN, sys, s, lane + 32 * q)] = qs[s];
+  for (int s = 0; s < kTcSlices; ++s) {
+    union {
+      Vec vec;
+      __nv_bfloat16 h[PER];
+    } u;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) u.h[i] = qs[i][s];
+    *reinterpret_cast<Vec*>(sy + tc_tile_index<D>(kTcN, sys, s, PER * static_cast<int>(lane))) = u.vec;
   }
 }
 
