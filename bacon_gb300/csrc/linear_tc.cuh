@@ -4,16 +4,22 @@
 //
 // Splitting (the Ozaki scheme): every row of A and every system's stage
 // vector (a column of Y) is scaled by a power of two so that its largest
-// entry is below 1, then cut into NS slices of 6 bits each:
-//     x = 2^e * sum_s q_s 2^(-6(s+1)),  q_s integer, |q_s| <= 63.
+// entry is below 1, then cut into NS = 5 slices of B = 8 bits each:
+//     x = 2^e * sum_s q_s 2^(-8(s+1)),  q_s integer, |q_s| <= 255.
 // Integers of at most 8 significant bits are exact in bf16, and a K = 256 dot
-// product of two slices is an integer below 256 * 63 * 63 < 2^20, so the
-// tensor cores compute every slice product exactly in FP32.  All pairs
-// (s, t) with s + t = d share the scale 2^(-6(d+2)); their sum stays below
-// 6 * 2^20 < 2^24 and is still exact, so one TMEM accumulator per diagonal d
-// (d = 0..NS-1) suffices.  The epilogue combines the NS diagonals in FP64,
-// applies 2^(e_row + e_sys) and the system's dt, and writes K_i.  Pairs with
-// s + t >= NS are dropped: the relative error of the product is ~2^(-6 NS).
+// product of two slices is an integer of magnitude at most 256 * 255^2 =
+// 16,646,400 < 2^24, so the tensor cores compute every slice product exactly
+// in FP32.  Pairs (s, t) with s + t = d share the scale 2^(-8(d+2)).  The
+// pairs of diagonals 0..2 (1 + 2 + 3) get one TMEM accumulator each, so their
+// sums are exact.  Diagonal 3's four pairs share one accumulator and diagonal
+// 4's five another: those sums can round in FP32 (at most ~2^26), but they
+// weigh at most 2^-24 of diagonal 0, so their rounding stays near 2^-40 of
+// the product.  Eight accumulators x 64 columns fill the 512 TMEM columns.
+// The epilogue combines them as 64-bit integers, applies 2^(e_row + e_sys)
+// and the system's dt, and writes K_i.  Pairs with s + t >= NS are dropped.
+// The relative error of the product is ~2^-39 (40-bit operands), with 15
+// slice products per K step; six 6-bit slices (exact sums in six
+// accumulators, 21 products) reached ~2^-35.
 //
 // CTA tile: 128 rows of A x 64 systems, K = D in chunks of 32 staged in
 // shared memory in the canonical no-swizzle K-major layout (8 x 16-byte core
@@ -29,12 +35,50 @@
 
 namespace bacon {
 
-constexpr int kTcSlices = 6;      // slices per operand (36 bits)
-constexpr int kTcBits = 6;        // bits per slice
+constexpr int kTcSlices = 5;      // slices per operand (40 bits)
+constexpr int kTcBits = 8;        // bits per slice
+constexpr int kTcFracBits = kTcSlices * kTcBits;
+constexpr int kTcAccs = 8;        // TMEM accumulators
+constexpr int kTcExactDiags = 3;  // diagonals 0..2 accumulate exactly, a pair per accumulator
 constexpr int kTcM = 128;         // rows per CTA
 constexpr int kTcN = 64;          // systems per CTA
 constexpr int kTcKc = 32;         // K per shared-memory chunk (two buffers)
-constexpr int kTcTmemCols = 512;  // kTcSlices accumulators x 64 columns, rounded to a power of two
+constexpr int kTcTmemCols = 512;  // kTcAccs accumulators x 64 columns, rounded to a power of two
+
+// Accumulator of the slice pair (s, t): one per pair on diagonals 0..2
+// (accumulators 0 | 1, 2 | 3, 4, 5), one per diagonal for 3 and 4 (6, 7);
+// the diagonal an accumulator holds; and the first s (in the MMA loop's
+// order) that writes it.
+__host__ __device__ constexpr int tc_acc(int s, int t) {
+  return s + t == 0 ? 0 : s + t == 1 ? 1 + s : s + t == 2 ? 3 + s : s + t == 3 ? 6 : 7;
+}
+__host__ __device__ constexpr int tc_acc_diag(int acc) {
+  return acc == 0 ? 0 : acc <= 2 ? 1 : acc <= 5 ? 2 : acc == 6 ? 3 : 4;
+}
+__host__ __device__ constexpr int tc_acc_first_s(int acc) {
+  return acc == 2 ? 1 : acc == 4 ? 1 : acc == 5 ? 2 : 0;
+}
+__host__ __device__ constexpr bool tc_split_exact(int k) {
+  // the accumulators of diagonals 0..2 take one pair each, at most
+  // k * 255^2, an exact FP32 integer; every accumulator index is in range
+  // and its first pair is the one tc_acc_first_s names
+  for (int acc = 0; acc < kTcAccs; ++acc) {
+    int pairs = 0, first = -1;
+    for (int s = 0; s < kTcSlices; ++s)
+      for (int t = 0; s + t < kTcSlices; ++t)
+        if (tc_acc(s, t) == acc) {
+          if (tc_acc_diag(acc) != s + t) return false;
+          if (first < 0) first = s;
+          ++pairs;
+        }
+    if (pairs == 0 || first != tc_acc_first_s(acc)) return false;
+    if (tc_acc_diag(acc) < kTcExactDiags && (pairs != 1 || static_cast<long long>(k) * 255 * 255 >= (1ll << 24)))
+      return false;
+  }
+  return true;
+}
+static_assert(tc_split_exact(256), "slice products must accumulate exactly in FP32 for K = 256");
+static_assert(kTcAccs * kTcN <= kTcTmemCols, "the accumulators fit the TMEM allocation");
 
 struct TcArgs {
   LinArgs st;
@@ -296,13 +340,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
               for (int s = 0; s < kTcSlices; ++s) {
 #pragma unroll
                 for (int t = 0; s + t < kTcSlices; ++t) {
-                  const int d = s + t;
+                  const int ac = tc_acc(s, t);
                   const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
                   const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
-                  // The first product into diagonal d is the pair (0, d) of
-                  // the first K step: it overwrites the accumulator.
-                  const uint32_t acc = (c == 0 && ks == 0 && s == 0) ? 0u : 1u;
-                  tc_mma(tmem + static_cast<uint32_t>(d * kTcN), ad, bd, idesc, acc);
+                  // The first product into an accumulator (its first pair
+                  // of the first K step) overwrites it.
+                  const uint32_t acc = (c == 0 && ks == 0 && s == tc_acc_first_s(ac)) ? 0u : 1u;
+                  tc_mma(tmem + static_cast<uint32_t>(ac * kTcN), ad, bd, idesc, acc);
                 }
               }
             }
@@ -355,20 +399,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
       tphase ^= 1u;
       if (!ok_sh) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // Diagonal d holds an exact integer below 2^23 scaled by 2^(-6(d+2)):
-      // the sum over d is an exact 64-bit integer times 2^-42.
+      // An accumulator of diagonal d holds an integer (exact below 2^24 for
+      // d <= 2, at most ~2^26.4 for d = 3, 4) scaled by 2^(-8(d+2)): the sum
+      // over the accumulators, each shifted by 8(4 - d), is a 64-bit integer
+      // (below 2^57) times 2^-48.
       long long acc[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) acc[j] = 0;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
 #pragma unroll
-        for (int d = 0; d < kTcSlices; ++d) {
+        for (int ac = 0; ac < kTcAccs; ++ac) {
           float v[16];
-          tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(d * kTcN + cbase + 16 * h), v);
+          tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(ac * kTcN + cbase + 16 * h),
+                    v);
 #pragma unroll
           for (int j = 0; j < 16; ++j)
-            acc[16 * h + j] += static_cast<long long>(__float2int_rz(v[j])) << (kTcBits * (kTcSlices - 1 - d));
+            acc[16 * h + j] += static_cast<long long>(__float2int_rz(v[j]))
+                               << (kTcBits * (kTcSlices - 1 - tc_acc_diag(ac)));
         }
       }
       // hand the accumulators back to the producer
@@ -410,10 +458,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
 }
 
 // Integer slicing.  With e the exponent of the largest |x| of a row (or a
-// system), |x| / 2^e < 1 and its first 36 fraction bits, F = floor(|x| *
-// 2^(36-e)), are the mantissa shifted right; slice s is bits 35-6s..30-6s of
-// F with the sign of x.  This equals truncating 64 r, r -= trunc, six times in
-// FP64 (every step of that is exact), without the FP64 instructions GB300
+// system), |x| / 2^e < 1 and its first 40 fraction bits, F = floor(|x| *
+// 2^(40-e)), are the mantissa shifted right; slice s is bits 39-8s..32-8s of
+// F with the sign of x.  This equals truncating 256 r, r -= trunc, five times
+// in FP64 (every step of that is exact), without the FP64 instructions GB300
 // runs at 1/64 of its integer rate.  Returns e for the largest magnitude bits.
 __device__ __forceinline__ int tc_exponent_of(unsigned long long max_abs_bits) {
   // max_abs_bits = bits of the largest |x|; e with |x| < 2^e, 0 for zero
@@ -427,13 +475,13 @@ __device__ __forceinline__ void tc_slices(double x, int e, __nv_bfloat16 (&q)[kT
   const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
   const int ex = static_cast<int>((b >> 52) & 0x7ff);
   const unsigned long long m = (b & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
-  // |x| = m * 2^(ex' - 1075) with ex' = max(ex, 1); F = m * 2^(ex' - 1075 + 36 - e)
-  const int sh = 1075 - 36 + e - (ex ? ex : 1);  // right shift, >= 17 since |x| < 2^e
+  // |x| = m * 2^(ex' - 1075) with ex' = max(ex, 1); F = m * 2^(ex' - 1075 + 40 - e)
+  const int sh = 1075 - kTcFracBits + e - (ex ? ex : 1);  // right shift, >= 13 since |x| < 2^e
   const unsigned long long F = sh >= 64 ? 0ull : (m >> sh);
   const bool neg = (b >> 63) != 0ull;
 #pragma unroll
   for (int s = 0; s < kTcSlices; ++s) {
-    const int v = static_cast<int>((F >> (30 - 6 * s)) & 63ull);
+    const int v = static_cast<int>((F >> (kTcFracBits - kTcBits * (s + 1))) & ((1ull << kTcBits) - 1ull));
     q[s] = __float2bfloat16_rz(static_cast<float>(neg ? -v : v));
   }
 }

@@ -40,15 +40,16 @@ def test_linear_fma_close_to_exact_solution(engine):
 
 @pytest.mark.parametrize("dim", [128, 256])
 def test_linear_tensor_core_split(engine, dim):
-    """tcgen05 stage GEMM with 6 x 6-bit bf16 slices: each product term is
-    exact to ~2^-36 relative, so the engine reaches the FP64 engine's
-    accuracy against the exact solution.  The embedded error estimate is
-    ~1e9 times smaller than |K| here (tol 1e-8, |A y| ~ 10), so it carries a
-    ~1 % perturbation, and with the reference's safety factor 1 (a rejection
-    lands the next attempt at err ~ tol) that flips some accept decisions:
-    measured 2 % (dim 128) and 11 % (dim 256) of systems differ by a few
-    accepted steps, where the FMA engine (1e-16 perturbations) differs on
-    none."""
+    """tcgen05 stage GEMM with 5 x 8-bit bf16 slices: each product is
+    within ~2^-39 relative, so the engine reaches the FP64 engine's accuracy
+    against the exact solution.  The embedded error estimate is ~1e9 times
+    smaller than |K| here (tol 1e-8, |A y| ~ 10), so it carries a ~1e-3
+    relative perturbation, and with the reference's safety factor 1 (a
+    rejection lands the next attempt at err ~ tol) that can flip an accept
+    decision.  Measured: accepted counts equal the FP64 engine's on 100 %
+    (dim 128) and 99.7 % (dim 256) of systems, off by at most one step, and
+    final states within 1.5e-9 of it.  Six 6-bit slices (~2^-35) had
+    flipped 11 % at dim 256."""
     b = W.linear_shared(n=1024, dim=dim, seed=23)
     ex = b.extra["exact"](5.0)
     fp = _solve(engine, b, precision=0)
@@ -59,7 +60,7 @@ def test_linear_tensor_core_split(engine, dim):
     same_tc = np.mean(tc.accepted == fp.accepted)
     same_fma = np.mean(fma.accepted == fp.accepted)
     assert same_fma >= 0.99, same_fma
-    assert same_tc >= 0.8, (same_tc, same_fma)
-    assert np.abs(tc.accepted.astype(np.int64) - fp.accepted).max() <= 4
+    assert same_tc >= 0.97, (same_tc, same_fma)
+    assert np.abs(tc.accepted.astype(np.int64) - fp.accepted).max() <= 2
     # different accept decisions on a few systems move their states by ~tol
-    assert np.abs(tc.y - fp.y).max() < 5e-8
+    assert np.abs(tc.y - fp.y).max() < 2e-8
