@@ -64,3 +64,43 @@ def test_linear_tensor_core_split(engine, dim):
     assert np.abs(tc.accepted.astype(np.int64) - fp.accepted).max() <= 2
     # different accept decisions on a few systems move their states by ~tol
     assert np.abs(tc.y - fp.y).max() < 2e-8
+
+
+def _exact_at(b, t_end):
+    """Q diag(exp(-lambda t_i)) Q^T y0_i for each system's own end time."""
+    q, lam = b.extra["Q"], b.extra["lambda"]
+    z = q.T @ b.y0
+    return q @ (np.exp(-lam[:, None] * t_end[None, :]) * z)
+
+
+def test_linear_ragged_batch_end_times_exact(engine, oracle):
+    """37 systems (the control kernel serves four per warp, so the last warp
+    is partly empty) with per-system end times, so systems stop in different
+    rounds: bit-identical to the oracle."""
+    b = W.linear_shared(n=37, dim=64, seed=31)
+    t_end = np.random.default_rng(5).uniform(1.0, 5.0, 37)
+    sol = engine.rk_solve(b.y0, None, b.t0, t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=2, precision=0, shared=b.extra["A"])
+    assert sol.code == 0
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+    ref = oracle.rk_solve_batch(cfg, b.rhs, b.y0, None, b.t0, t_end, shared=b.extra["A"])
+    np.testing.assert_array_equal(sol.accepted, ref["accepted"])
+    np.testing.assert_array_equal(sol.rejected, ref["rejected"])
+    np.testing.assert_array_equal(sol.t, ref["t"])
+    np.testing.assert_array_equal(sol.y, ref["y"])
+
+
+def test_linear_tensor_core_ragged_tiles(engine):
+    """1,000 systems fill 15 tiles of 64 and leave the 16th with 40; per-system
+    end times retire systems from tiles in different rounds, so tiles run
+    partly live and, at the end, are skipped by both the producer warp and
+    the epilogue warps.  Every system ends at its own t_end within the
+    split's accuracy of the exact solution."""
+    b = W.linear_shared(n=1000, dim=128, seed=32)
+    t_end = np.random.default_rng(6).uniform(1.0, 5.0, 1000)
+    tc = engine.rk_solve(b.y0, None, b.t0, t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                         layout=2, precision=engine.TC_SPLIT, shared=b.extra["A"])
+    assert tc.code == 0 and (tc.status == 0).all()
+    # the last step is clamped to end - t, so t lands on t_end to rounding
+    assert (tc.t >= t_end).all() and np.allclose(tc.t, t_end, rtol=1e-12, atol=0.0)
+    assert np.abs(tc.y - _exact_at(b, tc.t)).max() < 1e-7
