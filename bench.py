@@ -273,8 +273,9 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
                          "statuses_ok": bool((tc.status == 0).all().item())},
         "fp64_fma": {"value": sub / fp_s, "unit": "solves/s", "n": sub,
                      "max_abs_err_vs_exact": float(np.abs(fp.y.cpu().numpy() - exact).max())},
-        "what": "lock-step RKF45 rounds; stage GEMM 256x256 x 256xN on tcgen05 (bf16 6x6-bit slices, exact FP32 "
-                "accumulation) vs FP64 DFMA SIMT GEMM; wall time of the whole solve"}
+        "what": "lock-step RKF45 rounds; stage GEMM 256x256 x 256xN on tcgen05 (bf16 5x8-bit slices, FP32 "
+                "accumulation exact on the leading diagonals, ~2^-39 product error) vs FP64 DFMA SIMT GEMM; "
+                "wall time of the whole solve"}
 
     # Stiff batch, corrected BDF6, one launch: 65,536 Robertson systems (a
     # thread each) and 65,536 damped spring-mass chains of m ~ U{2..64} masses

@@ -98,8 +98,9 @@ typedef enum {
   BACON_FP64_FMA = 1,
   BACON_FP32_COMP = 2,
   /* BACON_RHS_LINEAR only: the stage GEMM on tcgen05 tensor cores, bf16
-   * integer slices of A and Y (6 x 6 bits, Ozaki splitting) with exact FP32
-   * accumulation, combined in FP64; relative error of A*Y ~ 2^-36. */
+   * integer slices of A and Y (5 x 8 bits, Ozaki splitting) with FP32
+   * accumulation, exact on the three leading diagonals, combined in FP64;
+   * relative error of A*Y ~ 2^-39. */
   BACON_TC_SPLIT = 3
 } bacon_precision;
 
