@@ -157,6 +157,7 @@ SIGNATURES = {
     "bacon_ctx_kernel_launches": (ctypes.c_int64, [_VP]),
     "bacon_ctx_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "bacon_ctx_last_kernel_ms": (ctypes.c_int, [_VP, DP]),
+    "bacon_ctx_set_fault_injection": (ctypes.c_int, [_VP, ctypes.c_int]),
     "bacon_rk_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                       ctypes.POINTER(RkResult)]),
     "bacon_rk_solve_plain": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),

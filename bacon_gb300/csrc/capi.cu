@@ -109,6 +109,7 @@ int expected_params(int rhs, int dim) {
 
 struct bacon_ctx {
   int device = 0;
+  int fault_injection = BACON_FAULT_NONE;  // bacon_ctx_set_fault_injection
   cudaStream_t stream = nullptr;
   int num_sms = 0;
   // [0] work counter [1] first failing index [2] live [3] adjoint queue /
@@ -196,6 +197,14 @@ int bacon_ctx_destroy(bacon_ctx* c) {
 }
 
 int64_t bacon_ctx_kernel_launches(const bacon_ctx* c) { return c ? c->launches : 0; }
+
+int bacon_ctx_set_fault_injection(bacon_ctx* c, int kind) {
+  if (!c) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  if (kind != BACON_FAULT_NONE && kind != BACON_FAULT_TC_WITHHOLD)
+    return fail(BACON_INVALID_ARGUMENT, "unknown fault-injection kind");
+  c->fault_injection = kind;
+  return BACON_OK;
+}
 
 int bacon_ctx_stream(const bacon_ctx* c, void** stream) {
   if (!c || !stream) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
@@ -508,6 +517,10 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     ta.sy = c->tc_sy.as<__nv_bfloat16>();
     ta.ey = c->tc_ey.as<int32_t>();
     ta.error_flag = d_err;
+    // about one second at the SM clock; the fault-injection hook withholds
+    // the accumulator hand-off and shortens the waits to ~10 ms
+    ta.withhold_tmem_full = c->fault_injection == BACON_FAULT_TC_WITHHOLD ? 1 : 0;
+    ta.wait_limit = ta.withhold_tmem_full ? 20000000ll : 2000000000ll;
     BACON_CUDA(cudaMemsetAsync(c->d_ctl + 3, 0, sizeof(unsigned long long), c->stream));
     const double* Ap = A;
     __nv_bfloat16* sa = c->tc_sa.as<__nv_bfloat16>();

@@ -88,6 +88,8 @@ struct TcArgs {
   const int32_t* ey;        // [n]          system exponents
   int stage;
   unsigned int* error_flag; // set when a bounded wait gives up
+  long long wait_limit;     // SM clock cycles an mbarrier wait may take (about one second)
+  int withhold_tmem_full;   // fault injection for tests: the producer never signals the epilogue
 };
 
 // --- PTX wrappers -----------------------------------------------------------
@@ -127,12 +129,13 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                : "memory");
 }
 
-// Waits for the mbarrier phase with a time limit of about one second of SM
-// clock; on expiry it raises the error flag and returns false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase, unsigned int* error_flag) {
+// Waits for the mbarrier phase for at most `limit` SM clock cycles; on
+// expiry it raises the error flag and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase, unsigned int* error_flag,
+                                                  long long limit) {
   const long long start = clock64();
   for (;;) {
-    if (clock64() - start > 2000000000ll) break;
+    if (clock64() - start > limit) break;
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
         constexpr int64_t kAChunk = kTcSlices * kTcM * kTcKc, kBChunk = kTcSlices * kTcN * kTcKc;  // elements
         auto load = [&](int b, int c) {
           if (pending[b]) {
-            if (ok && !mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag)) ok = false;
+            if (ok && !mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag, a.wait_limit)) ok = false;
             phase[b] ^= 1u;
             pending[b] = false;
           }
@@ -315,12 +318,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
           const int buf = c & 1;
           if (c + 1 < kChunks) load(buf ^ 1, c + 1);
           if (ok) {
-            if (mbar_wait_bounded(smem_addr(&full_bar[buf]), fphase[buf], a.error_flag)) inflight[buf] = false;
+            if (mbar_wait_bounded(smem_addr(&full_bar[buf]), fphase[buf], a.error_flag, a.wait_limit)) inflight[buf] = false;
             else ok = false;
             fphase[buf] ^= 1u;
           }
           if (ok && c == 0 && !first) {
-            if (!mbar_wait_bounded(smem_addr(&tmem_empty), ephase, a.error_flag)) ok = false;
+            if (!mbar_wait_bounded(smem_addr(&tmem_empty), ephase, a.error_flag, a.wait_limit)) ok = false;
             ephase ^= 1u;
           }
           if (ok) {
@@ -352,7 +355,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
             }
             tc_commit(smem_addr(&mbar[buf]));
             pending[buf] = true;
-            if (c + 1 == kChunks) tc_commit(smem_addr(&tmem_full));
+            if (c + 1 == kChunks && !a.withhold_tmem_full) tc_commit(smem_addr(&tmem_full));
           }
         }
       }
@@ -364,10 +367,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
       // CTA's shared memory and tensor memory
 #pragma unroll
       for (int b = 0; b < 2; ++b)
-        if (pending[b]) mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag);
+        if (pending[b]) mbar_wait_bounded(smem_addr(&mbar[b]), phase[b], a.error_flag, a.wait_limit);
 #pragma unroll
       for (int b = 0; b < 2; ++b)
-        if (inflight[b]) mbar_wait_bounded(smem_addr(&full_bar[b]), fphase[b], a.error_flag);
+        if (inflight[b]) mbar_wait_bounded(smem_addr(&full_bar[b]), fphase[b], a.error_flag, a.wait_limit);
     }
   } else {
     // ---- epilogue ----------------------------------------------------------
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
       }
       tc_epi_sync();
       if (!(any_w[0] | any_w[1])) continue;  // the producer skips it too
-      if (tid == 0) ok_sh = mbar_wait_bounded(smem_addr(&tmem_full), tphase, a.error_flag) ? 1 : 0;
+      if (tid == 0) ok_sh = mbar_wait_bounded(smem_addr(&tmem_full), tphase, a.error_flag, a.wait_limit) ? 1 : 0;
       tc_epi_sync();
       tphase ^= 1u;
       if (!ok_sh) break;

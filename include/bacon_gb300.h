@@ -123,6 +123,15 @@ int bacon_ctx_stream(const bacon_ctx* ctx, void** stream);
 /* Device time in milliseconds of the last solve's main integration kernel,
  * from CUDA events recorded around it on the context's stream. */
 int bacon_ctx_last_kernel_ms(const bacon_ctx* ctx, double* ms);
+/* Test hook, no counterpart in the reference: makes the context's next
+ * solves take a failure path on purpose, so that tests can check how it is
+ * reported.  BACON_FAULT_TC_WITHHOLD: the tensor-core stage GEMM
+ * (BACON_TC_SPLIT) never signals that its accumulators are ready, so its
+ * epilogue's bounded wait runs out after ~10 ms; the solve returns
+ * BACON_CUDA_ERROR and the context stays usable.  BACON_FAULT_NONE turns it
+ * off.  Nothing faults or hangs the GPU. */
+typedef enum { BACON_FAULT_NONE = 0, BACON_FAULT_TC_WITHHOLD = 1 } bacon_fault;
+int bacon_ctx_set_fault_injection(bacon_ctx* ctx, int kind);
 
 /* ---- batch description -------------------------------------------------- */
 /* One solve of n independent systems of dimension `dim`.  All arrays are SoA

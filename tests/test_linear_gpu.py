@@ -104,3 +104,29 @@ def test_linear_tensor_core_ragged_tiles(engine):
     # the last step is clamped to end - t, so t lands on t_end to rounding
     assert (tc.t >= t_end).all() and np.allclose(tc.t, t_end, rtol=1e-12, atol=0.0)
     assert np.abs(tc.y - _exact_at(b, tc.t)).max() < 1e-7
+
+
+def test_linear_tensor_core_wait_runs_out_and_context_recovers(engine):
+    """Failure path of the tensor-core stage GEMM, without a GPU fault: the
+    context's fault-injection hook makes the producer withhold the
+    accumulator hand-off, so the epilogue's bounded mbarrier wait runs out
+    (~10 ms), the kernel sets its error flag and returns, and the solve
+    reports BACON_CUDA_ERROR.  With the hook off, the same context then
+    solves the batch bit-identically to a solve that never failed."""
+    from bacon_gb300 import _capi
+    b = W.linear_shared(n=64, dim=128, seed=33)
+    ctx = engine.Context(0)
+    ref = _solve(engine, b, precision=engine.TC_SPLIT)
+    lib = _capi.load()
+    assert lib.bacon_ctx_set_fault_injection(ctx.handle, 1) == 0
+    with pytest.raises(engine.IVPError) as err:
+        engine.rk_solve(b.y0, None, b.t0, b.t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                        layout=2, precision=engine.TC_SPLIT, shared=b.extra["A"], ctx=ctx)
+    assert "bounded mbarrier wait" in str(err.value)
+    assert lib.bacon_ctx_set_fault_injection(ctx.handle, 0) == 0
+    assert lib.bacon_ctx_set_fault_injection(ctx.handle, 7) != 0
+    again = engine.rk_solve(b.y0, None, b.t0, b.t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                            layout=2, precision=engine.TC_SPLIT, shared=b.extra["A"], ctx=ctx)
+    assert again.code == 0
+    np.testing.assert_array_equal(again.y, ref.y)
+    np.testing.assert_array_equal(again.accepted, ref.accepted)
