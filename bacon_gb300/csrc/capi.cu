@@ -25,10 +25,23 @@
 #include "plain.h"
 #include "registry.h"
 #include "rk_adjoint.cuh"
+#include <nvtx3/nvToolsExt.h>
 
 namespace bacon {
 double measure_fp64_fma_gflops(cudaStream_t stream, int num_sms);
 }
+
+namespace {
+// An NVTX range around each public solve, so a profiler's timeline (or
+// `ncu --nvtx --nvtx-include`) can attribute kernels to the call that
+// launched them.  NVTX is header-only and costs nothing without a tool.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+}  // namespace
 
 namespace {
 
@@ -592,6 +605,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
 
 extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                               bacon_rk_result* r) {
+  NvtxRange nvtx_range("bacon_rk_solve");
   if (c && opt && p && p->rhs == BACON_RHS_LINEAR) {
     int rc0 = bacon_rk_validate(p);
     if (rc0 != BACON_OK) return rc0;
@@ -751,6 +765,7 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
 
 extern "C" int bacon_rk_solve_plain(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                                     bacon_rk_result* r) {
+  NvtxRange nvtx_range("bacon_rk_solve_plain");
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   int rc = bacon_rk_validate(p);
   if (rc != BACON_OK) return rc;
@@ -845,6 +860,7 @@ extern "C" int bacon_rk_solve_plain(bacon_ctx* c, const bacon_problem* p, const 
 // Batched BDF (one system per thread, dim <= 8).
 extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon_bdf_options* opt,
                                bacon_rk_result* r) {
+  NvtxRange nvtx_range("bacon_bdf_solve");
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   int rc = bacon_rk_validate(p);
   if (rc != BACON_OK) return rc;
@@ -988,6 +1004,7 @@ int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double eul
 
 extern "C" int bacon_adams_solve(bacon_ctx* c, const bacon_problem* p, const bacon_adams_options* opt,
                                  bacon_rk_result* r) {
+  NvtxRange nvtx_range("bacon_adams_solve");
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   int rc = bacon_rk_validate(p);
   if (rc != BACON_OK) return rc;
@@ -997,6 +1014,7 @@ extern "C" int bacon_adams_solve(bacon_ctx* c, const bacon_problem* p, const bac
 
 extern "C" int bacon_euler_solve(bacon_ctx* c, const bacon_problem* p, double dt, const bacon_adams_options* opt,
                                  bacon_rk_result* r) {
+  NvtxRange nvtx_range("bacon_euler_solve");
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   if (!p) return fail(BACON_INVALID_ARGUMENT, "problem is NULL");
   if (!(dt > 0.0)) return fail(BACON_TIME_DELTA_OOB, "dt <= 0");
@@ -1047,6 +1065,7 @@ extern "C" int bacon_ragged_validate(const bacon_ragged_problem* g) {
 
 extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, const bacon_ragged_problem* g,
                                      const bacon_bdf_options* opt, bacon_rk_result* ur, bacon_ragged_result* gr) {
+  NvtxRange nvtx_range("bacon_bdf_solve_mixed");
   if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
   if (!up && !g) return fail(BACON_INVALID_ARGUMENT, "both parts are NULL");
   if (opt->method != BACON_BDF6 && opt->method != BACON_BDF2) return fail(BACON_INVALID_ARGUMENT, "unknown method");
@@ -1285,6 +1304,7 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
 // of launch shapes and caches the fastest for this kernel and batch size.
 extern "C" int bacon_rk_autotune(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                                  bacon_rk_result* r, int32_t* best_block, int32_t* best_blocks_per_sm) {
+  NvtxRange nvtx_range("bacon_rk_autotune");
   if (!c || !opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
   static const int kShapes[][2] = {{64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}};
   bacon_rk_options o = *opt;
@@ -1316,6 +1336,7 @@ extern "C" int bacon_rk_autotune(bacon_ctx* c, const bacon_problem* p, const bac
 // Discrete adjoint: recording forward pass, then the reverse kernel.
 extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                                       bacon_rk_result* r, bacon_adjoint* adj) {
+  NvtxRange nvtx_range("bacon_rk_solve_adjoint");
   if (!c || !opt || !adj) return fail(BACON_INVALID_ARGUMENT, "NULL context, options or adjoint");
   int rc = bacon_rk_validate(p);
   if (rc != BACON_OK) return rc;
