@@ -9,7 +9,13 @@
 // kernel needs (work counter, lowest-failing-index slot, longest-first order
 // and its sort counters) lives in one fixed device array in this file.  Every
 // GPU that loads the library holds that array (about 4 MiB) until the process
-// exits.
+// exits.  The CUDA runtime loads device code lazily, so the array and the
+// kernels are placed on a device by the first call there; a call with n == 0
+// does only that, for the kernel its options select.  Make that call before
+// the caller's memory pool reserves the GPU's memory.
+// The device address found then is kept for the life of the process: calls
+// must not span a cudaDeviceReset, which rebuilds the context and may move
+// the array.
 #include "bacon_gb300.h"
 
 #include <cuda_runtime.h>
@@ -115,10 +121,18 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
   for (const auto& e : g_kernels)
     if (e.key == key) fn = e.fn;
   if (!fn) return BACON_UNSUPPORTED;
-  if (p->n == 0) return BACON_OK;
 
+  // The address lookup places the scratch array on the current device (CUDA
+  // loads device code lazily), so it comes before the n == 0 return: a
+  // zero-size call is the warm-up that places the array and the kernels.
   unsigned char* scratch = nullptr;
   if (scratch_for_current_device(&scratch) != cudaSuccess) return BACON_CUDA_ERROR;
+  if (p->n == 0) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess || bacon::preload_lpt_order_kernels() != cudaSuccess)
+      return BACON_CUDA_ERROR;
+    return BACON_OK;
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0, num_sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -185,7 +199,8 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
     return BACON_CUDA_ERROR;
   if (first_fail == ~0ull) return BACON_OK;
   int32_t st = 0;
-  if (cudaMemcpy(&st, r->status + first_fail, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpyAsync(&st, r->status + first_fail, sizeof(st), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
     return BACON_CUDA_ERROR;
   return st;
 }

@@ -106,4 +106,15 @@ cudaError_t enqueue_lpt_order(const OrderArgs& a, int num_sms, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Forces the four kernels' device code onto the current device (the CUDA
+// runtime loads kernels lazily, at their first launch or query).
+cudaError_t preload_lpt_order_kernels() {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, span_minmax_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, span_histogram_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, span_scan_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, span_scatter_kernel);
+  return e;
+}
+
 }  // namespace bacon

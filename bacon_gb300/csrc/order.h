@@ -26,4 +26,8 @@ struct OrderArgs {
 // Enqueues the four kernels that fill a.order.  Needs n < 2^32.
 cudaError_t enqueue_lpt_order(const OrderArgs& a, int num_sms, cudaStream_t s);
 
+// Loads the order kernels' device code onto the current device now rather
+// than at their first launch.
+cudaError_t preload_lpt_order_kernels();
+
 }  // namespace bacon

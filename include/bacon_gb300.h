@@ -361,7 +361,13 @@ int bacon_ctx_last_reverse_ms(const bacon_ctx* ctx, double* ms);
  *     before any GPU work.
  *   - The first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  The CUDA runtime loads device code
+ *     lazily, so that first call is also what places the array and the
+ *     kernel on the device: make it before the caller's memory pool
+ *     reserves the GPU's memory.  A call with n == 0 does only this set-up
+ *     (for the kernel its options select) and is the cheap way to do it.
+ *   - The device address is kept for the life of the process; calls must
+ *     not span a cudaDeviceReset.
  *   - All calls share the one array, which keeps the last call's contents;
  *     each call resets what must start at zero.  Calls whose GPU work overlaps
  *     (other host threads or streams) race on it: serialize them.

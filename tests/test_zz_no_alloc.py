@@ -99,3 +99,33 @@ def test_noalloc_rejects_oversized_batch_and_host_memory(engine):
     assert L.bacon_rk_solve_noalloc(ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), None) == 17
     opts = engine.rk_options(layout=2, memory=engine.MEM_HOST)
     assert L.bacon_rk_solve_noalloc(ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), None) == 15
+
+
+def test_noalloc_zero_size_warm_up_then_no_device_memory_change(engine):
+    """A call with n == 0 is the documented warm-up (it places the scratch
+    array and the kernel on the device).  After it, a real call leaves the
+    device's free memory exactly as it was: the entry point allocates
+    nothing."""
+    import torch
+    from bacon_gb300 import _capi
+    L = _capi.load()
+    b = W.van_der_pol(n=4096, seed=17)
+    y0, prm = _device(b.y0), _device(b.params)
+    empty = engine.make_problem(y0[:, :0], prm[:, :0], 0.0, 10.0, b.tol, b.dt_min, b.dt_max, b.rhs)
+    opts = engine.rk_options(layout=2, memory=engine.MEM_DEVICE)
+    res0 = engine.make_result(engine.alloc_outputs(2, 0, device=True))
+    assert L.bacon_rk_solve_noalloc(ctypes.byref(empty), ctypes.byref(opts), ctypes.byref(res0), None) == 0
+    ref = engine.rk_solve(y0, prm, 0.0, 10.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
+    prob = engine.make_problem(y0, prm, 0.0, 10.0, b.tol, b.dt_min, b.dt_max, b.rhs)
+    outs = [engine.alloc_outputs(2, b.n, device=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for out in outs:
+        res = engine.make_result(out)
+        assert L.bacon_rk_solve_noalloc(ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    for out in outs:
+        _assert_same(out, ref)
+
