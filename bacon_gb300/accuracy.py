@@ -77,3 +77,50 @@ def final_state_error(y: np.ndarray, ref: np.ndarray) -> dict:
     rel = err / np.maximum(np.abs(ref).max(axis=0), 1e-300)
     return {"abs_median": float(np.median(err)), "abs_max": float(err.max()),
             "rel_median": float(np.median(rel)), "rel_max": float(rel.max()), "systems": int(err.size)}
+
+
+def chain_matrix(k: np.ndarray, c: float) -> np.ndarray:
+    """The constant Jacobian of a damped spring-mass chain with m = len(k)
+    unit masses (BACON_RHS_CHAIN): state (x_1..x_m, v_1..v_m), x' = v,
+    v_i' = k_i (x_{i-1} - x_i) + k_{i+1} (x_{i+1} - x_i) - c v_i with
+    x_0 = x_{m+1} = 0 and k_{m+1} = 0."""
+    m = len(k)
+    J = np.zeros((2 * m, 2 * m))
+    J[:m, m:] = np.eye(m)
+    for i in range(m):
+        kr = k[i + 1] if i + 1 < m else 0.0
+        J[m + i, i] = -(k[i] + kr)
+        if i > 0:
+            J[m + i, i - 1] = k[i]
+        if i + 1 < m:
+            J[m + i, i + 1] = kr
+        J[m + i, m + i] = -c
+    return J
+
+
+def chain_exact_final(y0: np.ndarray, params: np.ndarray, t: float) -> np.ndarray:
+    """Exact y(t) = expm(J t) y0 of one chain (params = k_1..k_m, c)."""
+    from scipy.linalg import expm
+    m = len(y0) // 2
+    return expm(chain_matrix(params[:m], float(params[m])) * t) @ y0
+
+
+def robertson_reference(y0: np.ndarray, params: np.ndarray, t_end: float, rtol: float = 1e-12,
+                        atol: float = 1e-14) -> np.ndarray:
+    """y(t_end) of one Robertson system (k1, k2, k3) with scipy's Radau and
+    the analytic Jacobian, at rtol 1e-12."""
+    from scipy.integrate import solve_ivp
+    k1, k2, k3 = (float(v) for v in params)
+
+    def f(t, y):
+        return [-k1 * y[0] + k3 * y[1] * y[2], k1 * y[0] - k2 * y[1] * y[1] - k3 * y[1] * y[2],
+                k2 * y[1] * y[1]]
+
+    def jac(t, y):
+        return [[-k1, k3 * y[2], k3 * y[1]], [k1, -2.0 * k2 * y[1] - k3 * y[2], -k3 * y[1]],
+                [0.0, 2.0 * k2 * y[1], 0.0]]
+
+    sol = solve_ivp(f, (0.0, t_end), np.asarray(y0, float), method="Radau", rtol=rtol, atol=atol, jac=jac)
+    if not sol.success:
+        raise RuntimeError(sol.message)
+    return sol.y[:, -1].copy()

@@ -36,3 +36,50 @@ def rk_flops(method: int, rhs: int, dim: int, attempts: int, accepted: int) -> i
     per, acc = flops_per_attempt(method, rhs, dim)
     return per * int(attempts) + acc * int(accepted)
 
+
+
+# flops of one vector-Jacobian product of the adjoint (Vjp<> in rhs.cuh)
+VJP_FLOPS = {5: 12, 6: 17, 7: 17}
+
+
+def adjoint_flops(method: int, rhs: int, dim: int, n_params: int, attempts: int, accepted: int) -> int:
+    """Forward recording pass plus the reverse kernel: per accepted step a
+    replay of the stages and the step update, then the reverse sweep (the
+    stage weights lam*b_s, one VJP per stage with dt scaling, the parameter
+    and state accumulations, and the transposed tableau products)."""
+    t = TABLEAUX[method]
+    D, S = dim, t["S"]
+    fwd = rk_flops(method, rhs, dim, attempts, accepted)
+    replay = 2 * D * t["nnz_a"] + S * (RHS_FLOPS[rhs] + D) + 2 * D * t["nnz_b"] + 1
+    sweep = S * D + S * (D + VJP_FLOPS[rhs] + n_params + D) + 2 * D * t["nnz_a"]
+    return fwd + int(accepted) * (replay + sweep)
+
+
+# flops of the chain right-hand side per state component and of the
+# analytic Jacobians of the stiff right-hand sides
+CHAIN_FLOPS_PER_COMPONENT = 3.5
+JAC_FLOPS = {8: 10, 9: 0}
+
+
+def bdf_flops(dim: int, rhs_flops: float, steps: float, newton_solves: float, newton_iters: float,
+              factorisations: float, jac_flops: float = 0.0, q: int = 6) -> float:
+    """Corrected BDF: per step the predictor and the error norm; per Newton
+    solve the Jacobian, the matrix I - h b_q J and the history constant; per
+    Newton iteration the right-hand side, the residual, the two triangular
+    substitutions (2 dim^2) and the update with its norm; per
+    factorisation the LU (2/3 dim^3) and the pivot reciprocals."""
+    n = float(dim)
+    per_step = 2 * n * (q + 1) + 3 * n + 1
+    per_solve = jac_flops + 2 * n * n + 2 * n * q
+    per_iter = rhs_flops + 3 * n + 2 * n * n + 3 * n + 1
+    per_fact = 2.0 * n ** 3 / 3.0 + n
+    return steps * per_step + newton_solves * per_solve + newton_iters * per_iter + factorisations * per_fact
+
+
+def linear_tc_flops(dim: int, attempts: int, stages: int = 6, slice_pairs: int = 15) -> tuple[float, float]:
+    """(bf16 tensor-core flops, FP64-equivalent flops) of the stage GEMMs of
+    the shared-matrix linear solve: every attempt of every system multiplies
+    its stage vector by A in each stage, as slice_pairs bf16 slice products
+    on the tensor cores, or one FP64 matrix-vector product of 2 dim^2."""
+    fp64 = float(attempts) * stages * 2.0 * dim * dim
+    return fp64 * slice_pairs, fp64

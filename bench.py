@@ -45,9 +45,9 @@ def parse():
     ap.add_argument("--n", type=int, default=1 << 20, help="systems per GPU")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="systems in the CPU sample")
     ap.add_argument("--skip-extras", action="store_true", help="skip plain/FMA/CPU side measurements")
-    ap.add_argument("--stiff-n", type=int, default=32768,
-                    help="systems of the stiff-batch side measurement (half Robertson, half chains); the "
-                         "workload's full size is 131072")
+    ap.add_argument("--stiff-n", type=int, default=131072,
+                    help="systems of the stiff-batch side measurement (half Robertson, half chains)")
+    ap.add_argument("--skip-tune", action="store_true", help="skip the autotuner before the timed region")
     ap.add_argument("--precision", default="fp64_exact", choices=["fp64_exact", "fp64_fma", "fp32_comp"],
                     help="arithmetic of the timed solve (the headline is fp64_exact)")
     return ap.parse_args()
@@ -163,10 +163,49 @@ def cpu_pool(fn, items, threads):
     return res, time.perf_counter() - t0
 
 
+def measured_peaks():
+    """The measured HBM and bf16 peaks of this GPU pool, or the
+    profiling recipe's fallback."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs"), "bf16_tflops": d.get("bf16_tflops"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def event_timed(torch, ext, fn, repeats, flush):
+    """Device time (ms) of fn on the engine's stream, `repeats` times, with an
+    L2 flush before each; returns the list."""
+    ms = []
+    for _ in range(repeats):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        fn()
+        e1.record(ext)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def ok_error(y, ref, status):
+    """Final-state error summary over the systems that ended with Done."""
+    from bacon_gb300 import accuracy as A
+    ok = np.asarray(status) == 0
+    if not ok.any():
+        return {"systems": 0}
+    return A.final_state_error(np.asarray(y)[:, ok], np.asarray(ref)[:, ok])
+
+
 def other_cpu_baselines(W):
     """The CPU restatement timed on bounded samples of the other workloads, on
     all host threads (reported baselines: the GPU numbers are measured on the
-    full workloads)."""
+    full workloads).  The stiff sample also returns the corrected BDF's work
+    counts (Newton solves and iterations, factorisations), the basis of the
+    stiff batch's algorithmic-flop model."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     out = {}
@@ -203,19 +242,71 @@ def other_cpu_baselines(W):
 
     def one(job):
         kind, i = job
+        O.bdf_work(reset=True)
         if kind == 0:
-            return O.bdf_solve_one(rcfg, rob.rhs, rob.y0[:, i], 0.0, 1e4, params=rob.params[:, i]).status
-        y0, p = ch.system(i)
-        return O.bdf_solve_one(ccfg, ch.rhs, y0, 0.0, 10.0, params=p).status
+            r = O.bdf_solve_one(rcfg, rob.rhs, rob.y0[:, i], 0.0, 1e4, params=rob.params[:, i])
+            dim = 3
+        else:
+            y0, p = ch.system(i)
+            r = O.bdf_solve_one(ccfg, ch.rhs, y0, 0.0, 10.0, params=p)
+            dim = len(y0)
+        w = O.bdf_work(reset=True)
+        w.update(kind=kind, dim=dim, steps=r.accepted + r.rejected, status=r.status)
+        return w
 
-    _, sec = cpu_pool(one, [(0, i) for i in ri] + [(1, i) for i in ci], threads)
+    work, sec = cpu_pool(one, [(0, i) for i in ri] + [(1, i) for i in ci], threads)
     out["bdf6_stiff"] = {"value": 2 * k / sec, "unit": "solves/s", "cores": threads,
                          "sample": f"{k} Robertson + {k} chains (evenly spaced) of the 131072-system batch"}
-    return out
+    return out, work
 
 
-def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
-    """The other benchmark workloads, one timed solve each (device-resident)."""
+def stiff_work_model(work):
+    """Per-part rates of the corrected BDF's work, from the CPU sample:
+    Newton solves and iterations per step, and factorisations per step
+    (Robertson: every Newton solve) or per chain (one per distinct h*b_q)."""
+    rates = {}
+    for kind in (0, 1):
+        ws = [w for w in work if w["kind"] == kind and w["status"] == 0]
+        steps = sum(w["steps"] for w in ws)
+        rates[kind] = {"solves_per_step": sum(w["newton_solves"] for w in ws) / steps,
+                       "iters_per_step": sum(w["newton_iters"] for w in ws) / steps,
+                       "fact_per_step": sum(w["factorisations"] for w in ws) / steps,
+                       "fact_per_system": sum(w["factorisations"] for w in ws) / len(ws),
+                       "systems": len(ws)}
+    return rates
+
+
+def stiff_roofline(R, rates, rob_steps, chain_dims, chain_steps, kernel_ms, fp64_peak_tflops):
+    """Algorithmic FP64 flops of the stiff launch from the GPU's own per-system
+    step counts and the CPU sample's work rates (a model: the Newton and
+    factorisation counts are the sample's averages)."""
+    r0, r1 = rates[0], rates[1]
+    steps = np.asarray(rob_steps, dtype=np.float64).sum()
+    flops = R.bdf_flops(3, R.RHS_FLOPS[8], steps, r0["solves_per_step"] * steps, r0["iters_per_step"] * steps,
+                        r0["fact_per_step"] * steps, jac_flops=R.JAC_FLOPS[8])
+    dims = np.asarray(chain_dims, dtype=np.float64)
+    cs = np.asarray(chain_steps, dtype=np.float64)
+    for d in np.unique(dims):
+        m = dims == d
+        st = cs[m].sum()
+        flops += R.bdf_flops(int(d), R.CHAIN_FLOPS_PER_COMPONENT * d, st, r1["solves_per_step"] * st,
+                             r1["iters_per_step"] * st, r1["fact_per_system"] * m.sum())
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    return {"bound": "fp64", "achieved": achieved, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak_tflops, "traffic": None, "flops_per_launch": flops,
+            "work": "model: GPU step counts per system x the CPU sample's Newton solves and iterations per step; "
+                    "per Newton iteration rhs + 2 dim^2 substitutions + 6 dim, per solve I - h b J (2 dim^2), per "
+                    "factorisation 2/3 dim^3 (Robertson: every Newton solve; chains: one per distinct h b_q, "
+                    "sample mean per chain) (bacon_gb300/roofline.py bdf_flops)",
+            "peak_source": "measured live (FP64 FMA probe kernel)"}
+
+
+def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n=131072):
+    """The other benchmark workloads, timed on the device (device-resident
+    inputs), each with its final-state error against an FP64 reference at
+    rtol 1e-12 and, where it has one, a roofline object."""
+    from bacon_gb300 import accuracy as A
+    from bacon_gb300 import roofline as R
     out = {}
 
     def to_dev(*xs):
@@ -223,20 +314,32 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
 
     # Van der Pol, 4096 systems, t in [0, 10] (the CPU-runnable workload).
     vb = W.van_der_pol()
+    vref = A.reference_final_states(vb)
     vy, vp = to_dev(vb.y0, vb.params)
     kw = dict(rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, layout=E.FEHLBERG, ctx=ctx)
     E.rk_solve(vy, vp, 0.0, 10.0, **kw)
-    s = E.rk_solve(vy, vp, 0.0, 10.0, **kw)
-    ms = ctx.last_kernel_ms()
-    out["van_der_pol_4096"] = {"value": vb.n / (ms * 1e-3), "unit": "solves/s", "kernel_ms": ms,
-                               "statuses_ok": bool((s.status == 0).all().item())}
+    kms = []
+    for _ in range(3):
+        s = E.rk_solve(vy, vp, 0.0, 10.0, **kw)
+        kms.append(ctx.last_kernel_ms())
+    ms = statistics.median(kms)
+    vacc = s.accepted.cpu().numpy().astype(np.int64)
+    vrej = s.rejected.cpu().numpy().astype(np.int64)
+    vfl = R.rk_flops(0, vb.rhs, 2, int(vacc.sum() + vrej.sum()), int(vacc.sum()))
+    out["van_der_pol_4096"] = {
+        "value": vb.n / (ms * 1e-3), "unit": "solves/s", "kernel_ms": ms,
+        "statuses_ok": bool((s.status == 0).all().item()),
+        "final_state_error_vs_rtol1e-12": ok_error(s.y.cpu().numpy(), vref, s.status.cpu().numpy()),
+        "roofline": {"bound": "fp64", "achieved": vfl / (ms * 1e-3) / 1e12, "peak": fp64_peak_tflops,
+                     "unit": "TFLOP/s", "frac": vfl / (ms * 1e-3) / 1e12 / fp64_peak_tflops,
+                     "note": "4096 threads fill 32 of the 152 SMs"}}
 
     # The same Van der Pol batch with Adams5 (the reference's predictor-
     # corrector, src/ivp/adams.rs): it restarts from an RK4 bootstrap after
-    # every dt change, so it takes ~10^5 step calls per system.
-    E.adams_solve(vy, vp, 0.0, 10.0, rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5, ctx=ctx)
-    a5 = E.adams_solve(vy, vp, 0.0, 10.0, rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5,
-                       ctx=ctx)
+    # every dt change, so it takes ~10^5..10^6 step calls per system.
+    akw = dict(rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5, ctx=ctx)
+    E.adams_solve(vy, vp, 0.0, 10.0, **akw)
+    a5 = E.adams_solve(vy, vp, 0.0, 10.0, **akw)
     ams = ctx.last_kernel_ms()
     st = a5.status.cpu().numpy()
     out["adams5_van_der_pol_4096"] = {
@@ -244,21 +347,20 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
         "status_counts": {int(k): int((st == k).sum()) for k in np.unique(st)},
         "step_calls_mean": float((a5.accepted.double() + a5.rejected.double()).mean().item()),
         "step_calls_max": float((a5.accepted.double() + a5.rejected.double()).max().item()),
-        "note": "the reference's Adams5 restarts from an RK4 bootstrap after every dt change (~7e5 step calls "
-                "per system on average here, step_calls_max for the slowest) and one thread runs each system's "
-                "steps serially, each dependent FP64 operation ~64 cycles: the launch lasts as long as the slowest "
-                "system, and 4096 systems fill 32 of 152 SMs, so a larger batch, not this one, is where the GPU "
-                "pays off"}
+        "final_state_error_vs_rtol1e-12": ok_error(a5.y.cpu().numpy(), vref, st),
+        "note": "status 8 = MinimumTimeDeltaExceeded, as the reference's Adams5 ends on these systems (bit-identical "
+                "to the CPU restatement); the launch lasts as long as the slowest system"}
 
     # Linear y' = A y, shared A (n = 256), 65,536 states, tol 1e-8.
     lb = W.linear_shared()
     ly, lA = to_dev(lb.y0, lb.extra["A"])
     lk = dict(rhs=lb.rhs, tol=lb.tol, dt_min=lb.dt_min, dt_max=lb.dt_max, layout=E.FEHLBERG, ctx=ctx, shared=lA)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    tc = E.rk_solve(ly, None, 0.0, 5.0, precision=E.TC_SPLIT, **lk)
-    torch.cuda.synchronize()
-    tc_s = time.perf_counter() - t0
+    lout = E.alloc_outputs(256, lb.n, device=True)
+    E.rk_solve(ly, None, 0.0, 5.0, precision=E.TC_SPLIT, out=lout, **lk)
+    tc_ms = event_timed(torch, ext, lambda: E.rk_solve(ly, None, 0.0, 5.0, precision=E.TC_SPLIT, out=lout, **lk),
+                        2, flush)
+    tc_s = min(tc_ms) * 1e-3
+    tc = E.Solution(lout["y"], lout["t"], lout["accepted"], lout["rejected"], lout["status"], 0)
     sub = 8192
     sy_, = to_dev(lb.y0[:, :sub])
     torch.cuda.synchronize()
@@ -267,19 +369,29 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
     torch.cuda.synchronize()
     fp_s = time.perf_counter() - t0
     exact = lb.extra["exact"](5.0, slice(0, sub))
+    att = int(tc.accepted.double().sum().item() + tc.rejected.double().sum().item())
+    bf16_fl, fp64_fl = R.linear_tc_flops(256, att)
+    peaks = measured_peaks()
+    bf16_ach = bf16_fl / tc_s / 1e12
     out["linear_shared_A_256"] = {
-        "tensor_split": {"value": lb.n / tc_s, "unit": "solves/s", "n": lb.n,
+        "tensor_split": {"value": lb.n / tc_s, "unit": "solves/s", "n": lb.n, "solve_ms": tc_s * 1e3,
                          "max_abs_err_vs_exact_first_8192": float(np.abs(tc.y[:, :sub].cpu().numpy() - exact).max()),
-                         "statuses_ok": bool((tc.status == 0).all().item())},
+                         "statuses_ok": bool((tc.status == 0).all().item()),
+                         "roofline": {"bound": "tensor", "achieved": bf16_ach, "peak": peaks["bf16_tflops"],
+                                      "unit": "TFLOP/s", "frac": bf16_ach / peaks["bf16_tflops"],
+                                      "fp64_equivalent_tflops": fp64_fl / tc_s / 1e12,
+                                      "peak_source": f"bf16 burst, {peaks['source']} (MEASURED_PEAKS.json)",
+                                      "work": "15 bf16 slice products of 2*256^2 per system, stage and attempt; "
+                                              "whole solve (stage GEMMs, slicing, control) in the time"}},
         "fp64_fma": {"value": sub / fp_s, "unit": "solves/s", "n": sub,
                      "max_abs_err_vs_exact": float(np.abs(fp.y.cpu().numpy() - exact).max())},
         "what": "lock-step RKF45 rounds; stage GEMM 256x256 x 256xN on tcgen05 (bf16 5x8-bit slices, FP32 "
                 "accumulation exact on the leading diagonals, ~2^-39 product error) vs FP64 DFMA SIMT GEMM; "
-                "wall time of the whole solve"}
+                "device time of the whole solve (CUDA events), error against the exact solution"}
 
-    # Stiff batch, corrected BDF6, one launch: 65,536 Robertson systems (a
-    # thread each) and 65,536 damped spring-mass chains of m ~ U{2..64} masses
-    # (dim 4..128, a warp each, factors in shared memory).
+    # Stiff batch, corrected BDF6, one launch: Robertson systems (a thread
+    # each) and damped spring-mass chains of m ~ U{2..64} masses (dim 4..128,
+    # warp groups with factors in shared memory).
     rob, ch = W.stiff_batch(stiff_n)
     u = W.Batch(rob.name, rob.rhs, *to_dev(rob.y0, rob.params, rob.t0, rob.t_end), rob.tol, rob.dt_min, rob.dt_max,
                 rob.seed)
@@ -291,18 +403,29 @@ def other_workloads(E, W, ctx, dev, torch, stiff_n=131072):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ms = ctx.last_kernel_ms()
+    ri = np.linspace(0, rob.n - 1, 8).astype(int)
+    rref = np.stack([A.robertson_reference(rob.y0[:, i], rob.params[:, i], 1e4) for i in ri], axis=1)
+    ci = np.linspace(0, ch.n - 1, 32).astype(int)
+    ry = rs.y.cpu().numpy()
+    cerr = max(float(np.abs(ry[ch.y_off[i]:ch.y_off[i + 1]] - A.chain_exact_final(*ch.system(i), 10.0)).max())
+               for i in ci)
     out["bdf6_stiff"] = {
         "value": stiff_n / (ms * 1e-3), "unit": "solves/s", "n": stiff_n, "kernel_ms": ms, "wall_s": wall,
         "sample": "full workload" if stiff_n == 131072 else
-                  f"{stiff_n} of the workload's 131072 systems, same generator and mix (--stiff-n 131072 for all)",
+                  f"{stiff_n} of the workload's 131072 systems, same generator and mix",
         "robertson": {"n": rob.n, "t_end": 1e4, "statuses_ok": bool((us.status == 0).all().item()),
                       "accepted_mean": float(us.accepted.double().mean().item())},
         "spring_chains": {"n": ch.n, "dims": "4..128 (m ~ U{2..64} masses)", "t_end": 10.0,
                           "statuses_ok": bool((rs.status == 0).all().item()),
                           "accepted_mean": float(rs.accepted.double().mean().item())},
+        "final_state_error_vs_rtol1e-12": {
+            "robertson_vs_radau": A.final_state_error(us.y.cpu().numpy()[:, ri], rref),
+            "chains_vs_expm_abs_max": cerr, "sample": "8 Robertson (Radau rtol 1e-12), 32 chains (exact expm)"},
         "what": "corrected BDF6 (Newton, analytic Jacobian, partial-pivot LU) in one launch: Robertson one "
-                "system per thread, chains one per warp with LU factors in shared memory and a 16-entry "
-                "factor cache per warp; bit-identical to the CPU restatement (tests/test_bdf_ragged_gpu.py)"}
+                "system per thread, chains by warp groups with LU factors in shared memory and a 16-entry "
+                "factor cache per warp; bit-identical to the CPU restatement (tests/test_bdf_ragged_gpu.py)",
+        "_steps": {"robertson": (us.accepted.long() + us.rejected.long()).cpu().numpy(),
+                   "chains": (rs.accepted.long() + rs.rejected.long()).cpu().numpy(), "dims": ch.dims}}
     return out
 
 
@@ -328,6 +451,7 @@ def main():
     ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
     b = workload(args.n, rank)
     fp64_peak = ctx.fp64_peak_gflops()
+    peak = fp64_peak / 1e3
 
     y0 = torch.from_numpy(b.y0).to(dev)
     prm = torch.from_numpy(b.params).to(dev)
@@ -343,6 +467,13 @@ def main():
                           layout=E.FEHLBERG, precision=precision, out=dst or out, ctx=ctx,
                           raise_on_error=True)
 
+    # The autotuner times its candidate launch shapes on this batch and caches
+    # the fastest in the context; the timed solves below use it.
+    cfg_line = config(args, b)
+    if not args.skip_tune:
+        bb, bs = E.rk_autotune(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                               layout=E.FEHLBERG, precision=prec, ctx=ctx, out=out)
+        cfg_line["launch_shape"] = {"autotuned": True, "block": bb, "blocks_per_sm": bs}
     for _ in range(max(args.warmup, 0)):
         solve()
     torch.cuda.synchronize()
@@ -386,7 +517,6 @@ def main():
     flops = R.rk_flops(0, b.rhs, 3, attempts, int(acc.sum()))
     kavg = sum(kern_ms) / len(kern_ms)
     achieved = flops / (kavg * 1e-3) / 1e12
-    peak = fp64_peak / 1e3
     traffic = None
     prof = os.path.join(ROOT, "profiles", "rk_persistent_lorenz_1m.json")
     if os.path.exists(prof):
@@ -419,74 +549,112 @@ def main():
     assert np.array_equal(hout["y"], out["y"].cpu().numpy()), "host and device paths disagree"
 
     extras = {}
+    summary = {}
     if not args.skip_extras:
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
+        from bacon_gb300 import accuracy as A
+        from bacon_gb300 import workloads as W
+
+        # FP64 with contracted multiply-adds, same workload.
         fout = E.alloc_outputs(3, b.n, device=True)
-        s0 = time.perf_counter()
         solve(E.FP64_FMA, fout)
-        torch.cuda.synchronize()
-        extras["fp64_fma_mode"] = {"value": b.n / (time.perf_counter() - s0), "unit": UNIT,
+        fms = event_timed(torch, ext, lambda: solve(E.FP64_FMA, fout), 2, flush)
+        extras["fp64_fma_mode"] = {"value": b.n / (min(fms) * 1e-3), "unit": UNIT,
                                    "note": "same workload, products and sums contracted (not bit-exact)"}
+
+        # The plain one-launch-per-attempt GPU RK45 on the same GPU and inputs:
+        # one warm-up solve, then three solves timed by CUDA events on the
+        # engine's stream (its host loop syncs once per attempt round).
         pout = E.alloc_outputs(3, b.n, device=True)
-        torch.cuda.synchronize()
-        s0 = time.perf_counter()
-        E.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
-                   layout=E.FEHLBERG, out=pout, ctx=ctx, plain=True, raise_on_error=True)
-        torch.cuda.synchronize()
-        plain_s = time.perf_counter() - s0
+
+        def plain():
+            E.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                       layout=E.FEHLBERG, out=pout, ctx=ctx, plain=True, raise_on_error=True)
+
+        plain()
+        pms = event_timed(torch, ext, plain, 3, flush)
+        plain_value = b.n / (statistics.median(pms) * 1e-3)
         same = bool(torch.equal(pout["y"], out["y"]))
         extras["plain_gpu_baseline"] = {
-            "value": b.n / plain_s, "unit": UNIT, "identical_results": same,
-            "what": "one launch per attempt, state in HBM, dense tableau, host loop until done"}
-        extras["speedup_vs_plain"] = value / world / (b.n / plain_s)
+            "value": plain_value, "unit": UNIT, "identical_results": same, "ms": pms,
+            "what": "one launch per attempt, state in HBM, dense tableau, host loop until done; 1 warm-up, "
+                    "median of 3 CUDA-event timings"}
+        speedup_plain = value / world / plain_value
+        extras["speedup_vs_plain"] = speedup_plain
 
         # FP32-stage mode (float-float stages, FP64 control), same workload.
         cout = E.alloc_outputs(3, b.n, device=True)
         solve(E.FP32_COMP, cout)
-        comp_ms = []
-        for _ in range(2):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            solve(E.FP32_COMP, cout)
-            comp_ms.append(ctx.last_kernel_ms())
-        comp_value = b.n / (min(comp_ms) * 1e-3)
+        comp_ms = event_timed(torch, ext, lambda: solve(E.FP32_COMP, cout), 3, flush)
+        comp_value = b.n / (statistics.median(comp_ms) * 1e-3)
         extras["fp32_comp_mode"] = {"value": comp_value, "unit": UNIT,
                                     "speedup_vs_fp64_exact": comp_value / (value / world),
-                                    "speedup_vs_plain": comp_value / (b.n / plain_s),
+                                    "speedup_vs_plain": comp_value / plain_value,
                                     "what": "float-float stages on the FP32 pipe, FP64 accept test and dt"}
 
-        # Final-state error against FP64 DOP853 at rtol 1e-12 (sample: T <= 5).
-        from bacon_gb300 import accuracy as A
-        short = np.flatnonzero(b.t_end <= 5.0)[:32]
-        sb = b.subset(short)
-        ref = A.reference_final_states(sb)
+        # The reference's literal tableau read row by row (1859/4014 kept):
+        # its error estimate is O(dt), so at tol 1e-6 the systems run into the
+        # attempt cap.  Timed on the headline's 16,384-system sample.
+        rng = np.random.default_rng(123)
+        sidx = np.sort(rng.choice(b.n, size=min(args.cpu_sample, b.n), replace=False))
+        sb = b.subset(sidx)
+        sy0, sprm, st0, ste = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+                               for x in (sb.y0, sb.params, sb.t0, sb.t_end))
+        aw = E.rk_solve(sy0, sprm, st0, ste, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                        layout=E.AS_WRITTEN, max_attempts=100000, ctx=ctx)
+        aw_ms = ctx.last_kernel_ms()
+        awst = aw.status.cpu().numpy()
+        aw_att = float(aw.accepted.double().sum().item() + aw.rejected.double().sum().item())
+        extras["as_written_tableau"] = {
+            "status_counts": {int(k): int((awst == k).sum()) for k in np.unique(awst)},
+            "attempts_per_s": aw_att / (aw_ms * 1e-3), "kernel_ms": aw_ms, "max_attempts": 100000,
+            "sample": f"{sb.n} systems of the headline batch",
+            "what": "status 13 = attempt cap: with 1859/4014 (src/ivp/rk.rs:499) the error estimate does not "
+                    "shrink with dt; bit-identical to the oracle (tests/test_rk_gpu.py::test_as_written_bit_exact)"}
+
+        # Final-state error against FP64 DOP853 at rtol 1e-12 (Lorenz is chaotic:
+        # the sample is the systems with T <= 5).
+        short = np.flatnonzero(b.t_end <= 5.0)[:64]
+        lsb = b.subset(short)
+        lref = A.reference_final_states(lsb)
         extras["final_state_error_vs_rtol1e-12"] = {
-            "fp64_exact": A.final_state_error(out["y"].cpu().numpy()[:, short], ref),
-            "fp32_comp": A.final_state_error(cout["y"].cpu().numpy()[:, short], ref),
+            "fp64_exact": A.final_state_error(out["y"].cpu().numpy()[:, short], lref),
+            "fp32_comp": A.final_state_error(cout["y"].cpu().numpy()[:, short], lref),
             "sample": f"{short.size} Lorenz systems with T <= 5 (chaotic: error grows with T)"}
 
         # Discrete adjoint (batched solve_ivp_adjoint) on the Lotka-Volterra workload.
-        from bacon_gb300 import workloads as W
         lv = W.lotka_volterra()
         ly0, lprm, ltg = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
                           for x in (lv.y0, lv.params, lv.extra["target"]))
         lout = E.alloc_outputs(2, lv.n, device=True)
         kw = dict(rhs=lv.rhs, tol=lv.tol, dt_min=lv.dt_min, dt_max=lv.dt_max, ctx=ctx, out=lout)
         E.rk_solve(ly0, lprm, 0.0, 15.0, layout=E.FEHLBERG, **kw)
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        E.rk_solve(ly0, lprm, 0.0, 15.0, layout=E.FEHLBERG, **kw)
-        fwd_ms = ctx.last_kernel_ms()
+        fwd = []
+        for _ in range(3):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            E.rk_solve(ly0, lprm, 0.0, 15.0, layout=E.FEHLBERG, **kw)
+            fwd.append(ctx.last_kernel_ms())
+        fwd_ms = statistics.median(fwd)
         adj = E.rk_solve_adjoint(ly0, lprm, 0.0, 15.0, ltg, layout=E.FEHLBERG, **kw)
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        s0 = time.perf_counter()
-        adj = E.rk_solve_adjoint(ly0, lprm, 0.0, 15.0, ltg, layout=E.FEHLBERG, **kw)
-        adj_wall = time.perf_counter() - s0
-        rec_ms, rev_ms = ctx.last_kernel_ms(), ctx.last_reverse_ms()
+        rec, rev, walls = [], [], []
+        for _ in range(3):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            adj = E.rk_solve_adjoint(ly0, lprm, 0.0, 15.0, ltg, layout=E.FEHLBERG, **kw)
+            walls.append(time.perf_counter() - s0)
+            rec.append(ctx.last_kernel_ms())
+            rev.append(ctx.last_reverse_ms())
+        rec_ms, rev_ms = statistics.median(rec), statistics.median(rev)
         adj_ms = rec_ms + rev_ms
         grad = torch.cat([adj.dl_dy0, adj.dl_dp]).cpu().numpy()
+        lacc = lout["accepted"].cpu().numpy().astype(np.int64)
+        lrej = lout["rejected"].cpu().numpy().astype(np.int64)
+        lst = lout["status"].cpu().numpy()
+        adj_fl = R.adjoint_flops(0, lv.rhs, 2, 4, int(lacc.sum() + lrej.sum()), int(lacc.sum()))
+        adj_ach = adj_fl / (adj_ms * 1e-3) / 1e12
+        lvs = np.arange(0, lv.n, lv.n // 4096)
+        lvref = A.reference_final_states(lv.subset(lvs))
         fd_rel = None
         if rank == 0:
             from oracle import oracle as O
@@ -501,46 +669,122 @@ def main():
         extras["adjoint"] = {
             "value": lv.n / (adj_ms * 1e-3), "unit": "grads/s", "workload": "Lotka-Volterra, 262144 systems, "
             "t in [0,15], tol 1e-7, loss = sum ||y(T)-target||^2, checkpoint every 32 accepted steps",
-            "e2e_value": lv.n / adj_wall, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+            "e2e_value": lv.n / min(walls), "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
             "record_forward_ms": rec_ms, "reverse_ms": rev_ms, "cost_vs_forward": adj_ms / fwd_ms,
-            "max_rel_diff_vs_frozen_central_fd_h1e-6": fd_rel, "fd_sample": 16}
-        extras.update(other_workloads(E, W, ctx, dev, torch, stiff_n=args.stiff_n))
+            "max_rel_diff_vs_frozen_central_fd_h1e-6": fd_rel, "fd_sample": 16,
+            "final_state_error_vs_rtol1e-12": ok_error(lout["y"].cpu().numpy()[:, lvs], lvref, lst[lvs]),
+            "roofline": {"bound": "fp64", "achieved": adj_ach, "peak": peak, "unit": "TFLOP/s",
+                         "frac": adj_ach / peak, "traffic": None, "flops_per_gradient_pass": adj_fl,
+                         "work": "recording forward pass (every attempt) + replay and reverse VJP sweep per "
+                                 "accepted step (bacon_gb300/roofline.py adjoint_flops)",
+                         "peak_source": "measured live (FP64 FMA probe kernel)"}}
+        extras.update(other_workloads(E, W, ctx, dev, torch, ext, flush, peak, stiff_n=args.stiff_n))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded numpy, Lorenz-63 batch)", "config": config(args, b),
+            "data": "synthetic (seeded numpy, Lorenz-63 batch)", "config": cfg_line,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_note": "DRAM reads of a 131,072-system capture scaled by 8 (reads only; the "
+                                         "results are written once and leave L2 after the kernel)",
                          "peak_source": "measured live (FP64 FMA probe kernel); MEASURED_PEAKS.json has no FP64 entry",
                          "flops_per_launch": flops, "kernel_ms": kavg,
                          "work": "194 flops per attempt + 25 per accepted attempt (bacon_gb300/roofline.py)"},
             "clocks": clocks.summary(), "wall_s_timed_region": wall,
             "statuses_ok": bool((status == 0).all()), "attempts_per_solve": attempts / b.n}
+    stiff_steps = extras.get("bdf6_stiff", {}).pop("_steps", None)
     line.update(extras)
 
     if rank == 0 and world == 1 and not args.skip_extras:
         from oracle import oracle as O
-        rng = np.random.default_rng(123)
-        idx = np.sort(rng.choice(b.n, size=min(args.cpu_sample, b.n), replace=False))
-        s = b.subset(idx)
+        s = b.subset(sidx)
         threads = os.cpu_count() or 1
         cfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_QRT, tol=s.tol, dt_min=s.dt_min, dt_max=s.dt_max)
         r = O.rk_solve_batch(cfg, s.rhs, s.y0, s.params, s.t0, s.t_end, threads=threads)
+        gy, gacc = out["y"].cpu().numpy()[:, sidx], acc[sidx]
         line["cpu_baseline"] = {
             "value": s.n / r["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{s.n} of the {b.n} Lorenz systems (seeded subset), all host threads",
-            "sample_bit_identical": bool(np.array_equal(r["y"], out["y"].cpu().numpy()[:, idx])
-                                         and np.array_equal(r["accepted"], acc[idx]))}
-        for name, base in other_cpu_baselines(W).items():
+            "sample_bit_identical": bool(np.array_equal(r["y"], gy) and np.array_equal(r["accepted"], gacc))}
+        # The same sample against the oracle with the platform pow(), the
+        # rounding of the reference's (tol/err).powf(1/4).
+        lcfg = O.rk_cfg(layout=O.FEHLBERG, pow_mode=O.POW_LIBM, tol=s.tol, dt_min=s.dt_min, dt_max=s.dt_max)
+        lr = O.rk_solve_batch(lcfg, s.rhs, s.y0, s.params, s.t0, s.t_end, threads=threads)
+        rel = np.abs(gy - lr["y"]).max(axis=0) / np.abs(lr["y"]).max(axis=0)
+        sh = s.t_end <= 10.0
+        line["parity_vs_reference_pow"] = {
+            "accepted_identical_frac": float(np.mean(gacc == lr["accepted"])),
+            "final_within_1e-9_frac": float(np.mean(rel <= 1e-9)),
+            "final_within_1e-9_frac_T_le_10": float(np.mean(rel[sh] <= 1e-9)),
+            "final_bit_identical_frac": float(np.mean(rel == 0.0)), "systems": int(s.n),
+            "note": "GPU (correctly rounded fourth root) vs the C restatement with the platform pow() on the "
+                    "headline's sample; a one-ulp dt difference grows like e^(0.9 t) on chaotic Lorenz, so the "
+                    "1e-9 bar is missed only at large T"}
+        base, work = other_cpu_baselines(W)
+        for name, bl in base.items():
             if isinstance(line.get(name), dict):
-                line[name]["cpu_baseline"] = base
+                line[name]["cpu_baseline"] = bl
+        if stiff_steps is not None and "bdf6_stiff" in line:
+            rates = stiff_work_model(work)
+            line["bdf6_stiff"]["roofline"] = stiff_roofline(
+                R, rates, stiff_steps["robertson"], stiff_steps["dims"], stiff_steps["chains"],
+                line["bdf6_stiff"]["kernel_ms"], peak)
+            line["bdf6_stiff"]["roofline"]["sample_rates"] = rates
+
+    if not args.skip_extras:
+        summary = compact_summary(line)
+        line["summary"] = summary
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def compact_summary(line):
+    """The side measurements in a few hundred bytes, as the last key of the
+    line: every figure is also in its full object above."""
+    def g(*path):
+        v = line
+        for k in path:
+            if not isinstance(v, dict) or k not in v:
+                return None
+            v = v[k]
+        return v
+
+    def r3(x):
+        return None if x is None else float(f"{x:.4g}")
+
+    return {
+        "lorenz_fp64_exact": {"solves_s": r3(line["value"]), "e2e": r3(g("e2e", "value")),
+                              "frac": r3(g("roofline", "frac"))},
+        "speedup_vs_plain": r3(g("speedup_vs_plain")), "plain_solves_s": r3(g("plain_gpu_baseline", "value")),
+        "fp32_comp_solves_s": r3(g("fp32_comp_mode", "value")),
+        "fp32_comp_vs_plain": r3(g("fp32_comp_mode", "speedup_vs_plain")),
+        "parity_pow": {"acc_identical": g("parity_vs_reference_pow", "accepted_identical_frac"),
+                       "within_1e-9": r3(g("parity_vs_reference_pow", "final_within_1e-9_frac")),
+                       "within_1e-9_T_le_10": r3(g("parity_vs_reference_pow", "final_within_1e-9_frac_T_le_10"))},
+        "adjoint": {"grads_s": r3(g("adjoint", "value")), "cost_vs_forward": r3(g("adjoint", "cost_vs_forward")),
+                    "fd_rel": r3(g("adjoint", "max_rel_diff_vs_frozen_central_fd_h1e-6")),
+                    "frac": r3(g("adjoint", "roofline", "frac"))},
+        "stiff": {"solves_s": r3(g("bdf6_stiff", "value")), "n": g("bdf6_stiff", "n"),
+                  "frac": r3(g("bdf6_stiff", "roofline", "frac"))},
+        "linear_tc": {"solves_s": r3(g("linear_shared_A_256", "tensor_split", "value")),
+                      "frac_bf16": r3(g("linear_shared_A_256", "tensor_split", "roofline", "frac"))},
+        "vdp_solves_s": r3(g("van_der_pol_4096", "value")), "adams5_solves_s": r3(g("adams5_van_der_pol_4096", "value")),
+        "final_state_rel_max_vs_rtol1e-12": {
+            "lorenz_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp64_exact", "rel_max")),
+            "lorenz_fp32comp_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp32_comp", "rel_max")),
+            "vdp": r3(g("van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
+            "adams5_vdp": r3(g("adams5_van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
+            "lv": r3(g("adjoint", "final_state_error_vs_rtol1e-12", "rel_max")),
+            "robertson_abs": r3(g("bdf6_stiff", "final_state_error_vs_rtol1e-12", "robertson_vs_radau", "abs_max")),
+            "chains_abs": r3(g("bdf6_stiff", "final_state_error_vs_rtol1e-12", "chains_vs_expm_abs_max")),
+            "linear_tc_abs": r3(g("linear_shared_A_256", "tensor_split", "max_abs_err_vs_exact_first_8192"))},
+        "cpu_16core_solves_s": r3(g("cpu_baseline", "value")),
+    }
 
 
 if __name__ == "__main__":

@@ -486,6 +486,33 @@ static void corrected_solve(int n, dmat M, const int* piv, const double* rinv, d
   }
 }
 
+/* Work counters of the corrected BDF on the calling thread, for the
+ * algorithmic-flop count of the benchmark's stiff roofline: Newton solves,
+ * Newton iterations, and factorisations a solver needs at the least (every
+ * solve for a right-hand side whose Jacobian depends on y; one per distinct
+ * h*b_q value of a solve for the linear chains, whose Jacobian is constant). */
+static __thread int64_t g_work[3];
+#define BDF_SEEN_MAX 4096
+static __thread double g_seen_hb[BDF_SEEN_MAX];
+static __thread int g_seen_n;
+
+void oracle_bdf_work(int64_t* out3, int reset) {
+  if (out3) memcpy(out3, g_work, sizeof(g_work));
+  if (reset) {
+    memset(g_work, 0, sizeof(g_work));
+    g_seen_n = 0;
+  }
+}
+
+static void count_factorisation(int32_t rhs, double hb) {
+  if (rhs == ORC_RHS_CHAIN) {
+    for (int i = 0; i < g_seen_n; ++i)
+      if (g_seen_hb[i] == hb) return;
+    if (g_seen_n < BDF_SEEN_MAX) g_seen_hb[g_seen_n++] = hb;
+  }
+  g_work[2]++;
+}
+
 /* Solve G(y) = y - dt*b*f(t1, y) + sum_j a_j H[j-1] = 0 by Newton with the
  * Jacobian at the initial guess (one LU).  Returns 1 on convergence. */
 static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const double* p,
@@ -505,9 +532,12 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
   oracle_rhs_jacobian(rhs, n, t1, y, p, shared, J);
   for (int r = 0; r < n; ++r)
     for (int k = 0; k < n; ++k) M[r][k] = ((r == k) ? 1.0 : 0.0) - (hb * J[r * n + k]);
+  g_work[0]++;
+  count_factorisation(rhs, hb);
   if (!corrected_factor(n, M, piv, rinv)) return 0;
   const int max_newton = cfg->max_iter > 0 ? cfg->max_iter : 8;
   for (int it = 0; it < max_newton; ++it) {
+    g_work[1]++;
     oracle_rhs(rhs, n, t1, y, p, shared, f);
     for (int d = 0; d < n; ++d) g[d] = (y[d] - (hb * f[d])) + c[d];
     /* solve M dx = -g */

@@ -153,6 +153,11 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
 /* The corrected BDF's linear solve on its own (a test hook): A (row-major,
  * n x n, n <= 128) x = b.  Returns 1, or 0 on an exactly zero pivot. */
 int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, double* x);
+/* Work of the corrected BDF on the calling thread since the last reset:
+ * out3 = {Newton solves, Newton iterations, factorisations needed at the
+ * least (one per distinct h*b_q of a solve for the constant-Jacobian chains,
+ * one per Newton solve otherwise)}.  reset != 0 zeroes the counters. */
+void oracle_bdf_work(int64_t* out3, int reset);
 
 /* ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) -- */
 typedef struct {

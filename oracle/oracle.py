@@ -108,6 +108,8 @@ def lib():
                 ctypes.c_double, ctypes.c_double, dp, dp, dp, lp, lp, dp, dp, ctypes.c_int64]
             L.oracle_corrected_linsolve.restype = ctypes.c_int
             L.oracle_corrected_linsolve.argtypes = [ctypes.c_int32, dp, dp, dp]
+            L.oracle_bdf_work.restype = None
+            L.oracle_bdf_work.argtypes = [lp, ctypes.c_int]
         if hasattr(L, "oracle_adams_solve_one"):
             L.oracle_rootn.restype = ctypes.c_double
             L.oracle_rootn.argtypes = [ctypes.c_double, ctypes.c_int]
@@ -301,6 +303,15 @@ def bdf_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0)
         n = min(a.value, traj_cap)
         tt, ty = tt[:n], ty[:n]
     return Path(st, t.value, y, a.value, r.value, tt, ty)
+
+
+def bdf_work(reset: bool = True) -> dict:
+    """Corrected-BDF work on the calling thread since the last reset:
+    Newton solves, Newton iterations and the factorisations needed at the
+    least (see oracle_bdf_work in oracle.h)."""
+    out = np.zeros(3, dtype=np.int64)
+    lib().oracle_bdf_work(out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(reset))
+    return {"newton_solves": int(out[0]), "newton_iters": int(out[1]), "factorisations": int(out[2])}
 
 
 # ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) ----

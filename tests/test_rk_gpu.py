@@ -205,3 +205,49 @@ def test_stuck_controller_jumps_to_the_cap(engine, oracle):
     assert list(sol.status[:2]) == [13, 13]
     np.testing.assert_array_equal(sol.accepted[:2] + sol.rejected[:2], [10_000_000, 10_000_000])
     np.testing.assert_array_equal(sol.accepted, ref["accepted"])
+
+
+def _bench_sample():
+    """The headline Lorenz workload's seeded 16,384-system CPU sample (the
+    same subset bench.py times on the host cores)."""
+    b = W.lorenz(n=1 << 20, seed=2)
+    rng = np.random.default_rng(123)
+    return b.subset(np.sort(rng.choice(b.n, size=16384, replace=False)))
+
+
+def test_lorenz_headline_sample_vs_reference_pow(engine, oracle):
+    """The headline workload against the oracle with the platform pow(), the
+    rounding of the reference's (tol/err).powf(1/4) (src/ivp/rk.rs:401).
+    The engine's fourth root is correctly rounded; glibc's pow differs from
+    it by one ulp on ~0.085 % of inputs, and on chaotic Lorenz a one-ulp dt
+    difference grows like e^(0.9 t).  Measured on this sample: identical
+    accepted-step counts on 100 % of systems, final states within 1e-9
+    relative on 98.5 % (100 % of the systems with T <= 10)."""
+    import os
+    s = _bench_sample()
+    cfg = oracle.rk_cfg(layout=2, pow_mode=oracle.POW_LIBM, tol=s.tol, dt_min=s.dt_min, dt_max=s.dt_max)
+    ref = oracle.rk_solve_batch(cfg, s.rhs, s.y0, s.params, s.t0, s.t_end, threads=os.cpu_count())
+    sol = _gpu_batch(engine, s, layout=2)
+    assert sol.code == 0 and (ref["status"] == 0).all()
+    assert np.mean(sol.accepted == ref["accepted"]) >= 0.99
+    rel = np.abs(sol.y - ref["y"]).max(axis=0) / np.abs(ref["y"]).max(axis=0)
+    assert np.mean(rel <= 1e-9) >= 0.98
+    short = s.t_end <= 10.0
+    assert np.mean(rel[short] <= 1e-9) == 1.0
+
+
+@pytest.mark.parametrize("kind", ["lorenz", "lotka_volterra"])
+def test_as_written_bit_exact(engine, oracle, kind):
+    """The reference's literal tableau read row by row (AS_WRITTEN, with the
+    1859/4014 of src/ivp/rk.rs:499).  Its embedded error estimate is O(dt)
+    instead of O(dt^5), so at these tolerances almost every system runs into
+    the attempt cap; the per-system counts, times and states at the cap are
+    still bit-identical to the oracle's."""
+    if kind == "lorenz":
+        b = W.lorenz(n=1 << 20).subset(np.arange(0, 1 << 20, 2048))  # 512 systems, T ~ U[1, 20]
+    else:
+        b = W.lotka_volterra(n=512, seed=41)
+    cap = 100000
+    ref = _oracle_batch(oracle, b, layout=1, max_attempts=cap)
+    sol = _gpu_batch(engine, b, layout=1, max_attempts=cap)
+    _assert_identical(sol, ref)
