@@ -137,6 +137,16 @@ class RaggedResult(ctypes.Structure):
     ]
 
 
+class DenseOutput(ctypes.Structure):
+    _fields_ = [
+        ("capacity", ctypes.c_int64),
+        ("t", ctypes.c_void_p),
+        ("y", ctypes.c_void_p),
+        ("offsets", ctypes.c_void_p),
+        ("total", ctypes.c_int64),
+    ]
+
+
 class Adjoint(ctypes.Structure):
     _fields_ = [
         ("target", ctypes.c_void_p),
@@ -178,6 +188,12 @@ SIGNATURES = {
     "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                               ctypes.POINTER(RkResult), ctypes.POINTER(Adjoint)]),
     "bacon_ctx_last_reverse_ms": (ctypes.c_int, [_VP, DP]),
+    "bacon_rk_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                            ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
+    "bacon_bdf_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(BdfOptions),
+                                             ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
+    "bacon_adams_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(AdamsOptions),
+                                               ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
     "bacon_rk_solve_noalloc": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                               ctypes.POINTER(RkResult), _VP]),
     "bacon_builder_new": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),

@@ -38,6 +38,7 @@ struct AdamsArgs {
   double* traj_y;
   int32_t traj_cap;
   int32_t dyn_dim;
+  const int64_t* traj_off;  // [n+1] packed offsets, or null: slabs of traj_cap
   unsigned long long* queue;
   unsigned long long* first_fail;
 };
@@ -351,8 +352,12 @@ __global__ void __launch_bounds__(128) adams_persistent_kernel(const AdamsArgs a
           ++rej;
           continue;
         }
-        if (a.traj_t != nullptr && acc < a.traj_cap) {
-          const int64_t slot = idx * a.traj_cap + acc;
+        if (a.traj_t != nullptr) {
+          const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
+          if (slot < 0) {
+            status = kStCapacity;  // the trajectory buffer is full: the item is not yielded
+            break;
+          }
           a.traj_t[slot] = it;
 #pragma unroll
           for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = iy[d];
@@ -403,8 +408,12 @@ __global__ void __launch_bounds__(128) euler_persistent_kernel(const AdamsArgs a
         ++steps;
         if (X::add(t, dt) >= end) dt = X::sub(end, t);
         Rhs::template eval<X>(t, y, p, f);
-        if (a.traj_t != nullptr && acc < a.traj_cap) {
-          const int64_t slot = idx * a.traj_cap + acc;
+        if (a.traj_t != nullptr) {
+          const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
+          if (slot < 0) {
+            status = kStCapacity;  // the trajectory buffer is full: the item is not yielded
+            break;
+          }
           a.traj_t[slot] = t;
 #pragma unroll
           for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = y[d];

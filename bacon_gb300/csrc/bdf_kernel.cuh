@@ -38,6 +38,7 @@ struct BdfArgs {
   double* traj_t;
   double* traj_y;
   int32_t traj_cap;
+  const int64_t* traj_off;  // [n+1] packed offsets, or null: slabs of traj_cap
   unsigned long long* queue;
   unsigned long long* first_fail;
 };
@@ -341,6 +342,10 @@ __device__ __forceinline__ void bdf_corrected_system(const BdfArgs& a, int64_t i
       for (int d = 0; d < D; ++d) diff[d] = O::mul(0.5, O::sub(yh[d], O::add(H[0][d], O::mul(h, f0[d]))));
       error = bdf_norm(diff, dyn);
     }
+    if (ok && error <= a.tol && a.traj_t != nullptr && traj_slot(a.traj_off, a.traj_cap, idx, acc) < 0) {
+      status = kStCapacity;  // the trajectory buffer is full: the item is not yielded
+      break;
+    }
     if (ok && error <= a.tol) {
       const int kk = (k < 7) ? k + 1 : 7;
       for (int i = kk - 1; i >= 1; --i)
@@ -350,8 +355,8 @@ __device__ __forceinline__ void bdf_corrected_system(const BdfArgs& a, int64_t i
       for (int d = 0; d < D; ++d) H[0][d] = yh[d];
       k = kk;
       t = t1;
-      if (a.traj_t != nullptr && acc < a.traj_cap) {
-        const int64_t slot = idx * a.traj_cap + acc;
+      if (a.traj_t != nullptr) {
+        const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
         a.traj_t[slot] = t;
 #pragma unroll
         for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = yh[d];
@@ -839,8 +844,12 @@ __global__ void __launch_bounds__(128) bdf_as_compiled_kernel(const BdfArgs a, i
         ++rej;
         continue;
       }
-      if (a.traj_t != nullptr && acc < a.traj_cap) {
-        const int64_t slot = idx * a.traj_cap + acc;
+      if (a.traj_t != nullptr) {
+        const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
+        if (slot < 0) {
+          status = kStCapacity;  // the trajectory buffer is full: the item is not yielded
+          break;
+        }
         a.traj_t[slot] = it_t;
 #pragma unroll
         for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = it_y[d];

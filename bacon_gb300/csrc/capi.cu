@@ -151,6 +151,13 @@ struct bacon_ctx {
   DevBuf lin_A, lin_y, lin_K, lin_t, lin_dt, lin_end, lin_att;
   DevBuf tc_sa, tc_ea, tc_sy, tc_ey;
   DevBuf rg_yoff, rg_poff, rg_y0, rg_p, rg_t0, rg_te, rg_yout, rg_tout, rg_acc, rg_rej, rg_st, rg_ord, rg_lu;
+  // Packed dense output: while dense_off is set, the solves write every
+  // yielded item of system i to [dense_off[i], dense_off[i+1]) of the device
+  // streams dense_t / dense_y (the second pass of the *_solve_dense calls).
+  const int64_t* dense_off = nullptr;
+  double* dense_t = nullptr;
+  double* dense_y = nullptr;
+  DevBuf dn_off, dn_t, dn_y;
 };
 
 extern "C" {
@@ -196,7 +203,9 @@ int bacon_ctx_destroy(bacon_ctx* c) {
                     &c->pl_t, &c->pl_dt, &c->pl_end, &c->pl_att, &c->pl_acc, &c->pl_rej, &c->pl_st,
                     &c->ord, &c->ord_scratch, &c->adj_dt, &c->adj_ck, &c->adj_tgt, &c->adj_loss,
                     &c->adj_gy, &c->adj_gp, &c->lin_A, &c->lin_y, &c->lin_K, &c->lin_t, &c->lin_dt,
-                    &c->lin_end, &c->lin_att, &c->tc_sa, &c->tc_ea, &c->tc_sy, &c->tc_ey})
+                    &c->lin_end, &c->lin_att, &c->tc_sa, &c->tc_ea, &c->tc_sy, &c->tc_ey, &c->rg_yoff,
+                    &c->rg_poff, &c->rg_y0, &c->rg_p, &c->rg_t0, &c->rg_te, &c->rg_yout, &c->rg_tout,
+                    &c->rg_acc, &c->rg_rej, &c->rg_st, &c->rg_ord, &c->rg_lu, &c->dn_off, &c->dn_t, &c->dn_y})
     b->release();
   if (c->ev2) cudaEventDestroy(c->ev2);
   if (c->ev3) cudaEventDestroy(c->ev3);
@@ -656,6 +665,11 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   a.traj_t = o.traj_t;
   a.traj_y = o.traj_y;
   a.traj_cap = (o.traj_t ? r->traj_cap : 0);
+  if (c->dense_off) {
+    a.traj_t = c->dense_t;
+    a.traj_y = c->dense_y;
+    a.traj_off = c->dense_off;
+  }
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
   a.order = nullptr;
@@ -901,6 +915,11 @@ extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon
   a.traj_t = o.traj_t;
   a.traj_y = o.traj_y;
   a.traj_cap = o.traj_t ? r->traj_cap : 0;
+  if (c->dense_off) {
+    a.traj_t = c->dense_t;
+    a.traj_y = c->dense_y;
+    a.traj_off = c->dense_off;
+  }
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
   int dyn = p->dyn_dim ? 1 : 0;
@@ -970,6 +989,11 @@ int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double eul
   a.traj_t = o.traj_t;
   a.traj_y = o.traj_y;
   a.traj_cap = o.traj_t ? r->traj_cap : 0;
+  if (c->dense_off) {
+    a.traj_t = c->dense_t;
+    a.traj_y = c->dense_y;
+    a.traj_off = c->dense_off;
+  }
   a.dyn_dim = p->dyn_dim ? 1 : 0;
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
@@ -1297,6 +1321,119 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   }
   if (un > 0) return batch_return_code(c, ur, host, uo);
   return BACON_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Dense output: every item the reference iterator yields, packed into one
+// (t, y) stream with CSR offsets (src/ivp.rs:209-238, collect_vec per
+// system).  Two passes: the first solve counts each system's items, a scan of
+// the counts gives the offsets, and the second solve, bit-identical to the
+// first, writes each item straight to its slot.
+namespace {
+
+struct DenseGuard {  // clears the context's dense override on every exit
+  bacon_ctx* c;
+  ~DenseGuard() {
+    c->dense_off = nullptr;
+    c->dense_t = nullptr;
+    c->dense_y = nullptr;
+  }
+};
+
+template <class Solve>
+int dense_two_pass(bacon_ctx* c, const bacon_problem* p, int memory, bacon_rk_result* r, bacon_dense_output* dz,
+                   Solve solve) {
+  if (!c || !p || !r || !dz) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  if (r->traj_t || r->traj_y) return fail(BACON_INVALID_ARGUMENT, "dense output replaces traj_t / traj_y: pass NULL");
+  if (dz->capacity < 0) return fail(BACON_INVALID_ARGUMENT, "capacity < 0");
+  if (p->n > 0 && !dz->offsets) return fail(BACON_INVALID_ARGUMENT, "offsets is NULL");
+  if (dz->capacity > 0 && (!dz->t || !dz->y)) return fail(BACON_INVALID_ARGUMENT, "t or y is NULL");
+  const bool host = memory == BACON_MEM_HOST;
+  // Pass 1: the solve alone, for the per-system item counts.
+  int rc = solve();
+  if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+  const std::string pass1_msg = g_last_error;
+  const size_t n = static_cast<size_t>(p->n);
+  std::vector<int32_t> counts(n);
+  if (n > 0) {
+    if (host) {
+      std::memcpy(counts.data(), r->accepted, n * sizeof(int32_t));
+    } else {
+      BACON_CUDA(cudaMemcpyAsync(counts.data(), r->accepted, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+      BACON_CUDA(cudaStreamSynchronize(c->stream));
+    }
+  }
+  std::vector<int64_t> off(n + 1);
+  off[0] = 0;
+  for (size_t i = 0; i < n; ++i) off[i + 1] = off[i] + counts[i];
+  dz->total = off[n];
+  if (n > 0) {
+    if (host) {
+      std::memcpy(dz->offsets, off.data(), (n + 1) * sizeof(int64_t));
+    } else {
+      BACON_CUDA(cudaMemcpyAsync(dz->offsets, off.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                 c->stream));
+      BACON_CUDA(cudaStreamSynchronize(c->stream));
+    }
+  }
+  if (off[n] > dz->capacity)
+    return fail(BACON_CAPACITY_EXCEEDED, "dense output needs " + std::to_string(off[n]) + " items, capacity is " +
+                                             std::to_string(dz->capacity));
+  if (off[n] == 0) {
+    g_last_error = pass1_msg;
+    return rc;
+  }
+  // Pass 2: the same solve, writing every item to its packed slot.
+  const size_t total = static_cast<size_t>(off[n]);
+  DenseGuard guard{c};
+  if (host) {
+    BACON_CUDA(c->dn_off.ensure((n + 1) * sizeof(int64_t)));
+    BACON_CUDA(c->dn_t.ensure(total * sizeof(double)));
+    BACON_CUDA(c->dn_y.ensure(total * p->dim * sizeof(double)));
+    BACON_CUDA(cudaMemcpyAsync(c->dn_off.p, off.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               c->stream));
+    c->dense_off = c->dn_off.as<int64_t>();
+    c->dense_t = c->dn_t.as<double>();
+    c->dense_y = c->dn_y.as<double>();
+  } else {
+    c->dense_off = dz->offsets;
+    c->dense_t = dz->t;
+    c->dense_y = dz->y;
+  }
+  const int rc2 = solve();
+  if (rc2 == BACON_CUDA_ERROR || rc2 == BACON_INVALID_ARGUMENT || rc2 == BACON_UNSUPPORTED) return rc2;
+  if (rc2 != rc) return fail(BACON_CUDA_ERROR, "dense output: the second pass ended differently from the first");
+  if (host) {
+    BACON_CUDA(cudaMemcpyAsync(dz->t, c->dense_t, total * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BACON_CUDA(cudaMemcpyAsync(dz->y, c->dense_y, total * p->dim * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+    BACON_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return rc2;
+}
+
+}  // namespace
+
+extern "C" int bacon_rk_solve_dense(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                    bacon_rk_result* r, bacon_dense_output* dense) {
+  NvtxRange nvtx_range("bacon_rk_solve_dense");
+  if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
+  if (p->rhs == BACON_RHS_LINEAR) return fail(BACON_UNSUPPORTED, "the linear engine records no trajectory");
+  return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_rk_solve(c, p, opt, r); });
+}
+
+extern "C" int bacon_bdf_solve_dense(bacon_ctx* c, const bacon_problem* p, const bacon_bdf_options* opt,
+                                     bacon_rk_result* r, bacon_dense_output* dense) {
+  NvtxRange nvtx_range("bacon_bdf_solve_dense");
+  if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
+  return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_bdf_solve(c, p, opt, r); });
+}
+
+extern "C" int bacon_adams_solve_dense(bacon_ctx* c, const bacon_problem* p, const bacon_adams_options* opt,
+                                       bacon_rk_result* r, bacon_dense_output* dense) {
+  NvtxRange nvtx_range("bacon_adams_solve_dense");
+  if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
+  return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_adams_solve(c, p, opt, r); });
 }
 
 // ---------------------------------------------------------------------------

@@ -183,9 +183,11 @@ __global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
 
       if (nn_lt(dt, dt_min) && (ok ? tn : t) < end) {
         fin = kStMinDt;
+      } else if (ok && a.traj_t != nullptr && traj_slot(a.traj_off, a.traj_cap, idx, acc) < 0) {
+        fin = kStCapacity;  // the trajectory buffer is full: the item is not yielded
       } else if (ok) {
-        if (a.traj_t != nullptr && acc < a.traj_cap) {
-          const int64_t slot = idx * a.traj_cap + acc;
+        if (a.traj_t != nullptr) {
+          const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
           a.traj_t[slot] = tn;
 #pragma unroll
           for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = ff_to_double(yn[d]);

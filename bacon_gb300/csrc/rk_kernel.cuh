@@ -16,6 +16,7 @@
 #include "device_math.cuh"
 #include "rhs.cuh"
 #include "tableau.cuh"
+#include "traj.cuh"
 
 namespace bacon {
 
@@ -44,9 +45,10 @@ struct RkArgs {
   int32_t* accepted;     // [n]
   int32_t* rejected;     // [n]
   int32_t* status;       // [n]
-  double* traj_t;        // [n][cap] or null
-  double* traj_y;        // [n][cap][D] or null
+  double* traj_t;        // [n][cap], the packed stream, or null
+  double* traj_y;        // [n][cap][D], the packed stream, or null
   int32_t traj_cap;
+  const int64_t* traj_off;  // [n+1] packed offsets, or null: slabs of traj_cap
   unsigned long long* queue;       // work counter, zero at launch
   unsigned long long* first_fail;  // lowest failing index, ~0 at launch
   const uint32_t* order;           // work order (a permutation of [0, n)) or null
@@ -245,6 +247,8 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
         fin = kStMinDt;  // the accepted state of this attempt is never yielded
       } else if (kRecord && ok && acc >= a.max_steps) {
         fin = kStCapacity;  // the step log is full
+      } else if (ok && a.traj_t != nullptr && traj_slot(a.traj_off, a.traj_cap, idx, acc) < 0) {
+        fin = kStCapacity;  // the trajectory buffer is full: the item is not yielded
       } else if (ok) {
         if constexpr (kRecord) {
           a.dt_log[idx * a.max_steps + acc] = dt_used;
@@ -255,8 +259,8 @@ __global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
             for (int d = 0; d < D; ++d) c[1 + d] = y[d];
           }
         }
-        if (a.traj_t != nullptr && acc < a.traj_cap) {
-          const int64_t slot = idx * a.traj_cap + acc;
+        if (a.traj_t != nullptr) {
+          const int64_t slot = traj_slot(a.traj_off, a.traj_cap, idx, acc);
           a.traj_t[slot] = tn;
 #pragma unroll
           for (int d = 0; d < D; ++d) a.traj_y[slot * D + d] = yn[d];

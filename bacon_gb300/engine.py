@@ -106,6 +106,7 @@ class Solution:
     code: int         # BACON_OK or the lowest failing system's status
     traj_t: Any = None
     traj_y: Any = None
+    traj_off: Any = None   # dense output: system i's items are [traj_off[i], traj_off[i+1])
 
 
 def _ptr(a) -> int | None:
@@ -197,12 +198,44 @@ def make_result(out, traj_cap=0):
     return r
 
 
+def _dense_call(fn, handle, prob, opts, out, device, dim, n, capacity):
+    """Calls a *_solve_dense entry point.  With capacity None it first asks
+    for the item count (capacity 0), then allocates exactly that.  Returns
+    (code, t, y, offsets)."""
+    if device:
+        import torch
+        dev = torch.device("cuda")
+        mk = lambda shape, dt: torch.empty(shape, dtype=dt, device=dev)  # noqa: E731
+        f64, i64 = torch.float64, torch.int64
+    else:
+        mk = lambda shape, dt: np.empty(shape, dtype=dt)  # noqa: E731
+        f64, i64 = np.float64, np.int64
+    off = mk(n + 1, i64)
+    res = make_result(out)
+    if capacity is None:
+        dz = _capi.DenseOutput()
+        dz.capacity, dz.t, dz.y, dz.offsets = 0, None, None, _ptr(off)
+        code = fn(handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), ctypes.byref(dz))
+        if code in (14, 15, 16):
+            raise IVPError(code, _capi.last_error())
+        capacity = int(dz.total)
+    t = mk(max(capacity, 1), f64)
+    y = mk((max(capacity, 1), dim), f64)
+    dz = _capi.DenseOutput()
+    dz.capacity, dz.t, dz.y, dz.offsets = int(capacity), _ptr(t), _ptr(y), _ptr(off)
+    code = fn(handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), ctypes.byref(dz))
+    total = int(dz.total)
+    return code, t[:total], y[:total], off
+
+
 def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
              precision=FP64_EXACT, max_attempts=0, traj_cap=0, ctx: Context | None = None,
              plain=False, block=0, blocks_per_sm=0, use_graph=True, dyn_dim=False, out=None,
-             raise_on_error=False, schedule=0, shared=None) -> Solution:
+             raise_on_error=False, schedule=0, shared=None, dense=False, dense_capacity=None) -> Solution:
     """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors.
-    ``shared``: the dim x dim matrix of BACON_RHS_LINEAR (row-major)."""
+    ``shared``: the dim x dim matrix of BACON_RHS_LINEAR (row-major).
+    ``dense``: every yielded item of every system, packed (bacon_rk_solve_dense):
+    the Solution's traj_t (total,), traj_y (total, dim) and traj_off (n+1,)."""
     ctx = ctx or default_context()
     device = _is_device(y0)
     if not device:
@@ -221,8 +254,14 @@ def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, la
                       block, blocks_per_sm, use_graph, schedule)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
-    res = make_result(out, traj_cap)
     lib = _capi.load()
+    if dense:
+        code, tt, ty, off = _dense_call(lib.bacon_rk_solve_dense, ctx.handle, prob, opts, out, device, dim, n,
+                                        dense_capacity)
+        if code in (14, 15, 16) or (raise_on_error and code != 0):
+            raise IVPError(code, _capi.last_error())
+        return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code), tt, ty, off)
+    res = make_result(out, traj_cap)
     fn = lib.bacon_rk_solve_plain if plain else lib.bacon_rk_solve
     code = fn(ctx.handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res))
     if code in (14, 15, 16) or (raise_on_error and code != 0):
@@ -315,8 +354,9 @@ BDF_AS_COMPILED, BDF_CORRECTED = 0, 1
 
 def bdf_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=BDF6, mode=BDF_CORRECTED,
               max_iter=0, max_steps=0, traj_cap=0, ctx: Context | None = None, block=0, blocks_per_sm=0,
-              dyn_dim=False, out=None, raise_on_error=False) -> Solution:
-    """Batched BDF6 / BDF2 solve (systems of dimension <= 8)."""
+              dyn_dim=False, out=None, raise_on_error=False, dense=False, dense_capacity=None) -> Solution:
+    """Batched BDF6 / BDF2 solve (systems of dimension <= 8); ``dense`` as
+    rk_solve (bacon_bdf_solve_dense)."""
     ctx = ctx or default_context()
     device = _is_device(y0)
     if not device:
@@ -334,6 +374,12 @@ def bdf_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=BDF6, m
     o.max_iter, o.max_steps, o.block, o.blocks_per_sm = int(max_iter), int(max_steps), int(block), int(blocks_per_sm)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
+    if dense:
+        code, tt, ty, off = _dense_call(_capi.load().bacon_bdf_solve_dense, ctx.handle, prob, o, out, device, dim, n,
+                                        dense_capacity)
+        if code in (14, 15, 16) or (raise_on_error and code != 0):
+            raise IVPError(code, _capi.last_error())
+        return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code), tt, ty, off)
     res = make_result(out, traj_cap)
     code = _capi.load().bacon_bdf_solve(ctx.handle, ctypes.byref(prob), ctypes.byref(o), ctypes.byref(res))
     if code in (14, 15, 16) or (raise_on_error and code != 0):
@@ -429,11 +475,13 @@ def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_s
 
 def adams_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order=5, max_attempts=0, traj_cap=0,
                 ctx: Context | None = None, block=0, blocks_per_sm=0, dyn_dim=False, out=None,
-                raise_on_error=False) -> Solution:
-    """Batched Adams5 / Adams3 predictor-corrector (src/ivp/adams.rs)."""
+                raise_on_error=False, dense=False, dense_capacity=None) -> Solution:
+    """Batched Adams5 / Adams3 predictor-corrector (src/ivp/adams.rs); ``dense``
+    as rk_solve (bacon_adams_solve_dense)."""
     return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=tol, dt_min=dt_min, dt_max=dt_max, order=order,
                        euler_dt=None, max_attempts=max_attempts, traj_cap=traj_cap, ctx=ctx, block=block,
-                       blocks_per_sm=blocks_per_sm, dyn_dim=dyn_dim, out=out, raise_on_error=raise_on_error)
+                       blocks_per_sm=blocks_per_sm, dyn_dim=dyn_dim, out=out, raise_on_error=raise_on_error,
+                       dense=dense, dense_capacity=dense_capacity)
 
 
 def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx: Context | None = None,
@@ -441,11 +489,12 @@ def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx:
     """Batched Euler with a fixed step dt (src/ivp.rs:240-485)."""
     return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=1.0, dt_min=dt, dt_max=dt, order=1, euler_dt=dt,
                        max_attempts=max_steps, traj_cap=traj_cap, ctx=ctx, block=block,
-                       blocks_per_sm=blocks_per_sm, dyn_dim=False, out=out, raise_on_error=raise_on_error)
+                       blocks_per_sm=blocks_per_sm, dyn_dim=False, out=out, raise_on_error=raise_on_error,
+                       dense=False, dense_capacity=None)
 
 
 def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler_dt, max_attempts, traj_cap, ctx,
-                block, blocks_per_sm, dyn_dim, out, raise_on_error) -> Solution:
+                block, blocks_per_sm, dyn_dim, out, raise_on_error, dense, dense_capacity) -> Solution:
     ctx = ctx or default_context()
     device = _is_device(y0)
     if not device:
@@ -464,8 +513,14 @@ def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler
     o.max_attempts, o.block, o.blocks_per_sm = int(max_attempts), int(block), int(blocks_per_sm)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
-    res = make_result(out, traj_cap)
     L = _capi.load()
+    if dense:
+        code, tt, ty, off = _dense_call(L.bacon_adams_solve_dense, ctx.handle, prob, o, out, device, dim, n,
+                                        dense_capacity)
+        if code in (14, 15, 16) or (raise_on_error and code != 0):
+            raise IVPError(code, _capi.last_error())
+        return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code), tt, ty, off)
+    res = make_result(out, traj_cap)
     if euler_dt is None:
         code = L.bacon_adams_solve(ctx.handle, ctypes.byref(prob), ctypes.byref(o), ctypes.byref(res))
     else:

@@ -119,6 +119,16 @@ pub struct bacon_ragged_result {
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug)]
+pub struct bacon_dense_output {
+    pub capacity: i64,
+    pub t: *mut f64,
+    pub y: *mut f64,
+    pub offsets: *mut i64,
+    pub total: i64,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
 pub struct bacon_adjoint {
     pub target: *const f64,
     pub loss: *mut f64,
@@ -192,6 +202,27 @@ extern "C" {
         adjoint: *mut bacon_adjoint,
     ) -> c_int;
     pub fn bacon_ctx_last_reverse_ms(ctx: *const bacon_ctx, ms: *mut f64) -> c_int;
+    pub fn bacon_rk_solve_dense(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_rk_options,
+        result: *mut bacon_rk_result,
+        dense: *mut bacon_dense_output,
+    ) -> c_int;
+    pub fn bacon_bdf_solve_dense(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_bdf_options,
+        result: *mut bacon_rk_result,
+        dense: *mut bacon_dense_output,
+    ) -> c_int;
+    pub fn bacon_adams_solve_dense(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_adams_options,
+        result: *mut bacon_rk_result,
+        dense: *mut bacon_dense_output,
+    ) -> c_int;
     pub fn bacon_rk_solve_noalloc(
         problem: *const bacon_problem,
         options: *const bacon_rk_options,

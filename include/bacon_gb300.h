@@ -50,7 +50,8 @@ typedef enum {
   BACON_CUDA_ERROR = 14,
   BACON_INVALID_ARGUMENT = 15,
   BACON_UNSUPPORTED = 16,
-  /* A system took more accepted steps than the adjoint's step log holds. */
+  /* A system took more accepted steps than a fixed buffer holds: the
+   * adjoint's step log, or a trajectory slab. */
   BACON_CAPACITY_EXCEEDED = 17
 } bacon_status;
 
@@ -177,8 +178,10 @@ typedef struct {
  * the number of items it yields, `rejected` the number of Redo results
  * (src/ivp.rs:227-237); status is 0 when the iterator ended with Done, else
  * the error it returned.  traj_t/traj_y (optional, NULL to skip) receive the
- * first traj_cap yielded items per system: traj_t[i*cap + k],
- * traj_y[(i*cap + k)*dim + d]. */
+ * yielded items per system: traj_t[i*cap + k], traj_y[(i*cap + k)*dim + d];
+ * a system with more than traj_cap items ends with BACON_CAPACITY_EXCEEDED
+ * when the next one would not fit (see bacon_rk_solve_dense for a packed
+ * stream sized to the steps each system takes). */
 typedef struct {
   double* y_final;        /* [dim][n] */
   double* t_final;        /* [n] */
@@ -319,6 +322,38 @@ int bacon_bdf_solve_mixed(bacon_ctx* ctx, const bacon_problem* uniform,
                           const bacon_bdf_options* options,
                           bacon_rk_result* uniform_result,
                           bacon_ragged_result* ragged_result);
+
+/* ---- dense output --------------------------------------------------------- */
+/* Every item the reference iterator yields, for every system: the batched
+ * counterpart of collect_vec (src/ivp.rs:209-238), which returns each
+ * accepted (t, y).  The items are packed into one stream with CSR offsets:
+ * system i's items, in yield order, are t[k] and y[k*dim .. (k+1)*dim) for k
+ * in [offsets[i], offsets[i+1]), so memory follows the steps each system
+ * takes, not n times the longest.  Same memory kind as the problem. */
+typedef struct {
+  int64_t capacity;  /* items t and y can hold (0: only count) */
+  double* t;         /* [capacity] */
+  double* y;         /* [capacity][dim] */
+  int64_t* offsets;  /* [n+1], written by the call */
+  int64_t total;     /* out: items of the whole batch, offsets[n] */
+} bacon_dense_output;
+
+/* bacon_rk_solve / bacon_bdf_solve / bacon_adams_solve with dense output.
+ * Two passes: the first solve counts each system's items, an exclusive scan
+ * of the counts gives the offsets, and a second solve (bit-identical to the
+ * first) writes each item to its slot.  If total > capacity the call returns
+ * BACON_CAPACITY_EXCEEDED after the first pass with `total`, `offsets` and
+ * the per-system results filled and t / y untouched: allocate `total` items
+ * and call again.  result->traj_t / traj_y must be NULL.  The fixed per-system
+ * slabs of bacon_rk_result (traj_t, traj_cap) remain; a system whose slab is
+ * full ends with BACON_CAPACITY_EXCEEDED instead of dropping items.  Not for
+ * BACON_RHS_LINEAR. */
+int bacon_rk_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_rk_options* options,
+                         bacon_rk_result* result, bacon_dense_output* dense);
+int bacon_bdf_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_bdf_options* options,
+                          bacon_rk_result* result, bacon_dense_output* dense);
+int bacon_adams_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_adams_options* options,
+                            bacon_rk_result* result, bacon_dense_output* dense);
 
 /* ---- discrete adjoint ---------------------------------------------------- */
 /* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with
