@@ -137,6 +137,19 @@ class RaggedResult(ctypes.Structure):
     ]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [
+        ("variant", ctypes.c_int32),
+        ("max_registers", ctypes.c_int32),
+        ("systems_per_warp", ctypes.c_int32),
+        ("block", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+        ("candidates", ctypes.c_int32),
+        ("best_ms", ctypes.c_double),
+        ("default_ms", ctypes.c_double),
+    ]
+
+
 class DenseOutput(ctypes.Structure):
     _fields_ = [
         ("capacity", ctypes.c_int64),
@@ -183,6 +196,10 @@ SIGNATURES = {
     "bacon_bdf_solve_mixed": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RaggedProblem),
                                              ctypes.POINTER(BdfOptions), ctypes.POINTER(RkResult),
                                              ctypes.POINTER(RaggedResult)]),
+    "bacon_rk_autotune_ex": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                            ctypes.POINTER(RkResult), ctypes.POINTER(TuneResult)]),
+    "bacon_rk_set_tuned": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                          ctypes.POINTER(TuneResult)]),
     "bacon_rk_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                          ctypes.POINTER(RkResult), I32P, I32P]),
     "bacon_rk_solve_adjoint": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),

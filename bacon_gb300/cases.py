@@ -6,6 +6,7 @@
     python -m bacon_gb300.cases linear --n 8192 [--precision tc_split]
     python -m bacon_gb300.cases adjoint --n 16384
     python -m bacon_gb300.cases vdp --n 4096
+    python -m bacon_gb300.cases adams --n 4096
 
 Each case generates the workload's seeded batch at the given size (the
 workload generators in workloads.py), solves it `--repeat` times through the
@@ -65,6 +66,12 @@ def run(case: str, n: int, precision: str, repeat: int) -> dict:
             s = E.rk_solve(y0, None, 0.0, 5.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
                            layout=E.FEHLBERG, precision=prec, ctx=ctx, shared=A)
             out["status"] = _counts(s.status)
+        elif case == "adams":
+            b = W.van_der_pol(n=n)
+            y0, p = _dev(torch, b.y0, b.params)
+            s = E.adams_solve(y0, p, 0.0, 10.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, order=5,
+                              ctx=ctx)
+            out["status"] = _counts(s.status)
         elif case == "adjoint":
             b = W.lotka_volterra(n=n)
             y0, p, tgt = _dev(torch, b.y0, b.params, b.extra["target"])
@@ -72,6 +79,7 @@ def run(case: str, n: int, precision: str, repeat: int) -> dict:
                                    dt_max=b.dt_max, ctx=ctx)
             out["status"] = _counts(a.forward.status)
             out["reverse_ms"] = ctx.last_reverse_ms()
+            out["record_ms"] = ctx.last_kernel_ms()
         elif case in ("stiff", "chains"):
             if case == "stiff":
                 rob, ch = W.stiff_batch(n)
@@ -93,7 +101,7 @@ def run(case: str, n: int, precision: str, repeat: int) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["lorenz", "vdp", "linear", "adjoint", "stiff", "chains"])
+    ap.add_argument("case", choices=["lorenz", "vdp", "adams", "linear", "adjoint", "stiff", "chains"])
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--precision", default="fp64_exact", choices=sorted(PRECISION))
     ap.add_argument("--repeat", type=int, default=1)

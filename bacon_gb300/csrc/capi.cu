@@ -138,7 +138,13 @@ struct bacon_ctx {
     cudaGraphExec_t exec = nullptr;
   };
   std::unordered_map<uint64_t, Graph> graphs;
-  std::unordered_map<uint64_t, std::pair<int, int>> tuned;
+  // Autotuned launch per (kernel, batch size): kernel variant, threads per
+  // block, persistent CTAs per SM.
+  struct Tuned {
+    int variant, block, bps;
+  };
+  std::unordered_map<uint64_t, Tuned> tuned;
+  int force_variant = -1;  // set by the autotuner while it times a variant
   int64_t launches = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last main kernel
   bool ev_valid = false;
@@ -634,7 +640,7 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
   const void* fn = nullptr;
   for (const auto& e : c->kernels)
-    if (e.key == key) fn = e.fn;
+    if (e.key == key && e.variant == 0) fn = e.fn;
   if (!fn) return fail(BACON_UNSUPPORTED, "no compiled kernel for this (method, layout, precision, rhs, dim)");
   if (p->n == 0) return BACON_OK;
   BACON_CUDA(cudaSetDevice(c->device));
@@ -691,12 +697,21 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   int block = opt->block > 0 ? opt->block : 0;
   int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 0;
   const uint64_t tkey = tune_key(key, p->n);
-  if (block == 0 && bps == 0) {
+  int variant = c->force_variant;
+  if (block == 0 && bps == 0 && variant < 0) {
     auto it = c->tuned.find(tkey);
     if (it != c->tuned.end()) {
-      block = it->second.first;
-      bps = it->second.second;
+      variant = it->second.variant;
+      block = it->second.block;
+      bps = it->second.bps;
     }
+  }
+  if (variant > 0) {
+    const void* vfn = nullptr;
+    for (const auto& e : c->kernels)
+      if (e.key == key && e.variant == variant) vfn = e.fn;
+    if (!vfn) return fail(BACON_UNSUPPORTED, "no such kernel variant for this key");
+    fn = vfn;
   }
   const bool ff = opt->precision == BACON_FP32_COMP;
   if (block == 0) block = ff ? 256 : 128;
@@ -741,6 +756,7 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   if (use_graph) {
     uint64_t h = fnv1a(&a, sizeof(a));
     h = fnv1a(&key, sizeof(key), h);
+    h = fnv1a(&fn, sizeof(fn), h);  // the kernel variant
     h = fnv1a(&grid, sizeof(grid), h);
     h = fnv1a(&block, sizeof(block), h);
     const void* hp[] = {p->y0, p->params, p->t0, p->t_end, r->y_final, r->t_final, r->accepted,
@@ -997,12 +1013,24 @@ int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double eul
   a.dyn_dim = p->dyn_dim ? 1 : 0;
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
-  const int block = opt->block > 0 ? opt->block : 128;
+  // One thread runs each system's steps in order, so a batch smaller than
+  // the GPU's thread slots is latency bound: each dependent FP64 operation
+  // costs ~64 cycles, and warps that share an SM also share its FP64 pipe.
+  // Such a batch is spread thin, down to one warp per SM, instead of filling
+  // a few SMs with 128-thread CTAs.
+  int block = opt->block > 0 ? opt->block : 128;
+  if (opt->block <= 0 && opt->blocks_per_sm <= 0) {
+    const int64_t per_sm = (p->n + c->num_sms - 1) / c->num_sms;
+    if (per_sm < 128) block = static_cast<int>(per_sm <= 32 ? 32 : (per_sm + 31) / 32 * 32);
+  }
   if (block % 32 != 0 || block > 128) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 128");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
   if (max_bps < 1) return fail(BACON_CUDA_ERROR, "kernel cannot be resident");
-  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : model_blocks_per_sm(p->n, c->num_sms, block, max_bps);
+  // Step counts differ by orders of magnitude between systems and the launch
+  // lasts as long as the slowest, so every system starts at once when the
+  // occupancy allows (no second round behind a slow first one).
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(c->num_sms) * bps;
   const long long need = (p->n + block - 1) / block;
@@ -1439,33 +1467,93 @@ extern "C" int bacon_adams_solve_dense(bacon_ctx* c, const bacon_problem* p, con
 // ---------------------------------------------------------------------------
 // Autotuner: times the persistent kernel on the caller's own batch for a set
 // of launch shapes and caches the fastest for this kernel and batch size.
-extern "C" int bacon_rk_autotune(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
-                                 bacon_rk_result* r, int32_t* best_block, int32_t* best_blocks_per_sm) {
+extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                    bacon_rk_result* r, bacon_tune_result* out) {
   NvtxRange nvtx_range("bacon_rk_autotune");
   if (!c || !opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
-  static const int kShapes[][2] = {{64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}};
-  bacon_rk_options o = *opt;
-  o.use_graph = 0;
-  double best_ms = 1e300;
-  int bb = 0, bs = 0;
-  for (const auto& sh : kShapes) {
-    o.block = sh[0];
-    o.blocks_per_sm = sh[1];
-    const int rc = bacon_rk_solve(c, p, &o, r);
-    if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
-    double ms = 0.0;
-    if (bacon_ctx_last_kernel_ms(c, &ms) != BACON_OK) return BACON_CUDA_ERROR;
-    if (ms < best_ms) {
-      best_ms = ms;
-      bb = sh[0];
-      bs = sh[1];
-    }
-  }
+  if (p->rhs == BACON_RHS_LINEAR) return fail(BACON_UNSUPPORTED, "the linear engine has no persistent kernel");
+  // Launch shapes (threads per block, CTAs per SM) per register budget: the
+  // default kernel over the whole range, the capped ones at the occupancies
+  // their budgets open up.
+  static const int kShapes[][2] = {{64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}, {256, 3}};
+  static const int kCappedShapes[][2] = {{128, 4}, {256, 2}, {256, 3}, {256, 4}};
   const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
   const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
-  c->tuned[tune_key(key, p->n)] = {bb, bs};
-  if (best_block) *best_block = bb;
-  if (best_blocks_per_sm) *best_blocks_per_sm = bs;
+  std::vector<int> variants{0};
+  for (const auto& e : c->kernels)
+    if (e.key == key && e.variant > 0) variants.push_back(e.variant);
+  bacon_rk_options o = *opt;
+  o.use_graph = 0;
+  double best_ms = 1e300, default_ms = 0.0;
+  int bv = 0, bb = 0, bs = 0, count = 0;
+  struct Restore {
+    bacon_ctx* c;
+    ~Restore() { c->force_variant = -1; }
+  } restore{c};
+  // The untuned default first (occupancy model, variant 0).
+  c->force_variant = 0;
+  o.block = 0;
+  o.blocks_per_sm = 0;
+  int rc = bacon_rk_solve(c, p, &o, r);
+  if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+  if (bacon_ctx_last_kernel_ms(c, &default_ms) != BACON_OK) return BACON_CUDA_ERROR;
+  for (int v : variants) {
+    c->force_variant = v;
+    const auto* shapes = v == 0 ? kShapes : kCappedShapes;
+    const int ns = v == 0 ? static_cast<int>(sizeof(kShapes) / sizeof(kShapes[0]))
+                          : static_cast<int>(sizeof(kCappedShapes) / sizeof(kCappedShapes[0]));
+    for (int k = 0; k < ns; ++k) {
+      o.block = shapes[k][0];
+      o.blocks_per_sm = shapes[k][1];
+      rc = bacon_rk_solve(c, p, &o, r);
+      if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+      double ms = 0.0;
+      if (bacon_ctx_last_kernel_ms(c, &ms) != BACON_OK) return BACON_CUDA_ERROR;
+      ++count;
+      if (ms < best_ms) {
+        best_ms = ms;
+        bv = v;
+        bb = shapes[k][0];
+        bs = shapes[k][1];
+      }
+    }
+  }
+  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{bv, bb, bs};
+  if (out) {
+    out->variant = bv;
+    out->max_registers = bacon::variant_max_registers(bv);
+    out->systems_per_warp = 32;
+    out->block = bb;
+    out->blocks_per_sm = bs;
+    out->candidates = count;
+    out->best_ms = best_ms;
+    out->default_ms = default_ms;
+  }
+  return BACON_OK;
+}
+
+extern "C" int bacon_rk_set_tuned(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                  const bacon_tune_result* t) {
+  if (!c || !opt || !p || !t) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
+  if (t->block % 32 != 0 || t->block < 32 || t->block > 256 || t->blocks_per_sm < 1)
+    return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32 in 32..256, blocks_per_sm >= 1");
+  const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
+  const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
+  bool found = false;
+  for (const auto& e : c->kernels)
+    if (e.key == key && e.variant == t->variant) found = true;
+  if (!found) return fail(BACON_UNSUPPORTED, "no such kernel variant for this (method, layout, precision, rhs, dim)");
+  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{t->variant, t->block, t->blocks_per_sm};
+  return BACON_OK;
+}
+
+extern "C" int bacon_rk_autotune(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                 bacon_rk_result* r, int32_t* best_block, int32_t* best_blocks_per_sm) {
+  bacon_tune_result t{};
+  const int rc = bacon_rk_autotune_ex(c, p, opt, r, &t);
+  if (rc != BACON_OK) return rc;
+  if (best_block) *best_block = t.block;
+  if (best_blocks_per_sm) *best_blocks_per_sm = t.blocks_per_sm;
   return BACON_OK;
 }
 
@@ -1568,6 +1656,17 @@ extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, cons
   b.ckpt_slots = slots;
   b.ckpt_every = every;
   b.queue = c->d_ctl + 3;
+  // The reverse pass replays each system's accepted steps: hand the systems
+  // out most steps first (the counts are known once the forward pass ends).
+  bacon::OrderArgs rev_oa{};
+  const bool rev_lpt = p->n < (1ll << 32);
+  if (rev_lpt) {
+    BACON_CUDA(c->ord.ensure(n * sizeof(uint32_t)));
+    BACON_CUDA(c->ord_scratch.ensure(sizeof(bacon::OrderScratch)));
+    rev_oa = bacon::OrderArgs{p->n, nullptr, nullptr, 0.0, 0.0, c->ord_scratch.as<bacon::OrderScratch>(),
+                              c->ord.as<uint32_t>(), o.acc};
+    b.order = rev_oa.order;
+  }
 
   const int block = opt->block > 0 ? opt->block : 128;
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
@@ -1575,7 +1674,9 @@ extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, cons
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fwd_bps, ent->fwd, block, 0));
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rev_bps, ent->rev, 128, 0));
   if (fwd_bps < 1 || rev_bps < 1) return fail(BACON_CUDA_ERROR, "adjoint kernels cannot be resident");
-  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 1;
+  // The recording pass is the forward solve plus its step log: the same
+  // occupancy model as bacon_rk_solve.
+  int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : model_blocks_per_sm(p->n, c->num_sms, block, fwd_bps);
   if (bps > fwd_bps) bps = fwd_bps;
   const long long need = (p->n + block - 1) / block;
   long long fgrid = static_cast<long long>(c->num_sms) * bps;
@@ -1599,6 +1700,7 @@ extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, cons
   BACON_CUDA(cudaLaunchKernel(ent->fwd, dim3(static_cast<unsigned>(fgrid)), dim3(block), fargs, 0, c->stream));
   BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
   BACON_CUDA(cudaEventRecord(c->ev2, c->stream));
+  if (rev_lpt) BACON_CUDA(bacon::enqueue_lpt_order(rev_oa, c->num_sms, c->stream));
   BACON_CUDA(cudaLaunchKernel(ent->rev, dim3(static_cast<unsigned>(rgrid)), dim3(128), rargs, 0, c->stream));
   BACON_CUDA(cudaEventRecord(c->ev3, c->stream));
   if (host) {
@@ -1611,7 +1713,7 @@ extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, cons
   }
   BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
-  c->launches += lpt ? 6 : 2;
+  c->launches += (lpt ? 6 : 2) + (rev_lpt ? 4 : 0);
   c->ev_valid = true;
   c->rev_valid = true;
   BACON_CUDA(cudaStreamSynchronize(c->stream));

@@ -119,7 +119,7 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
   const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
   const void* fn = nullptr;
   for (const auto& e : g_kernels)
-    if (e.key == key) fn = e.fn;
+    if (e.key == key && e.variant == 0) fn = e.fn;
   if (!fn) return BACON_UNSUPPORTED;
 
   // The address lookup places the scratch array on the current device (CUDA

@@ -16,6 +16,10 @@ namespace bacon {
 namespace {
 
 __device__ __forceinline__ double span_of(const OrderArgs& a, int64_t i) {
+  if (a.weight) {
+    const int32_t w = a.weight[i];
+    return w > 0 ? static_cast<double>(w) : 0.0;
+  }
   const double t0 = a.t0 ? a.t0[i] : a.t0_s;
   const double te = a.t_end ? a.t_end[i] : a.t_end_s;
   const double s = te - t0;

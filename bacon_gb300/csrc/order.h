@@ -21,6 +21,9 @@ struct OrderArgs {
   double t0_s, t_end_s;
   OrderScratch* scratch;
   uint32_t* order;      // [n] output permutation, longest span first
+  // When set, system i's span is weight[i] (a work count known beforehand,
+  // such as the accepted steps a reverse pass replays) instead of t_end - t0.
+  const int32_t* weight = nullptr;
 };
 
 // Enqueues the four kernels that fill a.order.  Needs n < 2^32.

@@ -20,7 +20,15 @@ struct RkKey {
 
 struct RkEntry {
   RkKey key;
-  const void* fn;  // __global__ void(RkArgs)
+  const void* fn;   // __global__ void(RkArgs)
+  int variant = 0;  // 0: the default kernel; >0: an autotuner alternative
+};
+
+// The autotuner's kernel variants of one key: a register budget set through
+// the launch bounds (max_registers, 0 = the compiler's choice).
+struct RkVariantInfo {
+  int variant;
+  int max_registers;
 };
 
 struct AdjEntry {
@@ -40,6 +48,9 @@ void register_rk45_exact_l2(std::vector<RkEntry>& v);
 void register_rk45_fma(std::vector<RkEntry>& v);
 void register_rk23(std::vector<RkEntry>& v);
 void register_rk_ff(std::vector<RkEntry>& v);
+void register_rk_variants(std::vector<RkEntry>& v);
+// Register budget of a variant id (variant 1: 80, 2: 64; 0: none).
+inline int variant_max_registers(int variant) { return variant == 1 ? 80 : variant == 2 ? 64 : 0; }
 void register_adjoint_rk45(std::vector<AdjEntry>& v);
 void register_adjoint_rk23(std::vector<AdjEntry>& v);
 
@@ -51,6 +62,7 @@ inline std::vector<RkEntry> all_rk_kernels() {
   register_rk45_fma(v);
   register_rk23(v);
   register_rk_ff(v);
+  register_rk_variants(v);
   return v;
 }
 

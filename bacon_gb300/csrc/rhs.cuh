@@ -252,15 +252,15 @@ struct Jac<RhsChain<N>> {
 };
 
 // ---- vector-Jacobian products for the discrete adjoint --------------------
-// ubar = J_f(y)^T v and pbar = (df/dp)(y)^T v.  The reference has no
-// gradients; these are evaluated in the same order as the CPU oracle's
-// rhs_vjp (oracle/adjoint_oracle.c) so that the adjoint is bit-reproducible.
+// ubar = J_f(y)^T v, and mu += (df/dp)(y)^T v.  The reference has no
+// gradients; this is the adjoint's own arithmetic, with fused multiply-adds
+// (one rounding each) in the same order as the CPU oracle's rhs_vjp
+// (oracle/adjoint_oracle.c), so that the adjoint is bit-reproducible.
 template <class R>
 struct Vjp;
 
 template <int D>
 struct Vjp<RhsExp<D>> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&)[D], const double*, const double (&v)[D],
                                               double (&ub)[D], double*) {
 #pragma unroll
@@ -270,7 +270,6 @@ struct Vjp<RhsExp<D>> {
 
 template <int D>
 struct Vjp<RhsDecay<D>> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&)[D], const double*, const double (&v)[D],
                                               double (&ub)[D], double*) {
 #pragma unroll
@@ -280,7 +279,6 @@ struct Vjp<RhsDecay<D>> {
 
 template <>
 struct Vjp<RhsHarmonic> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&)[2], const double*, const double (&v)[2],
                                               double (&ub)[2], double*) {
     ub[0] = -v[1];
@@ -290,46 +288,43 @@ struct Vjp<RhsHarmonic> {
 
 template <>
 struct Vjp<RhsVdp> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&y)[2], const double* p, const double (&v)[2],
-                                              double (&ub)[2], double* pb) {
-    const double mu = p[0];
-    const double w = Ops::sub(1.0, Ops::mul(y[0], y[0]));
-    ub[0] = Ops::mul(Ops::sub(Ops::mul(Ops::mul(Ops::mul(-2.0, mu), y[0]), y[1]), 1.0), v[1]);
-    ub[1] = Ops::add(v[0], Ops::mul(Ops::mul(mu, w), v[1]));
-    pb[0] = Ops::mul(Ops::mul(w, y[1]), v[1]);
+                                              double (&ub)[2], double* mu) {
+    const double m = p[0];
+    const double w = __fma_rn(-y[0], y[0], 1.0);
+    ub[0] = __dmul_rn(__fma_rn(__dmul_rn(__dmul_rn(-2.0, m), y[0]), y[1], -1.0), v[1]);
+    ub[1] = __fma_rn(__dmul_rn(m, w), v[1], v[0]);
+    mu[0] = __fma_rn(__dmul_rn(w, y[1]), v[1], mu[0]);
   }
 };
 
 template <>
 struct Vjp<RhsLorenz> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&y)[3], const double* p, const double (&v)[3],
-                                              double (&ub)[3], double* pb) {
+                                              double (&ub)[3], double* mu) {
     const double s = p[0], r = p[1], b = p[2];
-    ub[0] = Ops::add(Ops::add(Ops::mul(-s, v[0]), Ops::mul(Ops::sub(r, y[2]), v[1])), Ops::mul(y[1], v[2]));
-    ub[1] = Ops::add(Ops::sub(Ops::mul(s, v[0]), v[1]), Ops::mul(y[0], v[2]));
-    ub[2] = Ops::sub(Ops::mul(-y[0], v[1]), Ops::mul(b, v[2]));
-    pb[0] = Ops::mul(Ops::sub(y[1], y[0]), v[0]);
-    pb[1] = Ops::mul(y[0], v[1]);
-    pb[2] = -Ops::mul(y[2], v[2]);
+    ub[0] = __fma_rn(y[1], v[2], __fma_rn(__dsub_rn(r, y[2]), v[1], __dmul_rn(-s, v[0])));
+    ub[1] = __fma_rn(y[0], v[2], __fma_rn(s, v[0], -v[1]));
+    ub[2] = __fma_rn(-y[0], v[1], -__dmul_rn(b, v[2]));
+    mu[0] = __fma_rn(__dsub_rn(y[1], y[0]), v[0], mu[0]);
+    mu[1] = __fma_rn(y[0], v[1], mu[1]);
+    mu[2] = __fma_rn(-y[2], v[2], mu[2]);
   }
 };
 
 template <>
 struct Vjp<RhsLotka> {
-  template <class Ops>
   __device__ __forceinline__ static void eval(const double (&y)[2], const double* p, const double (&v)[2],
-                                              double (&ub)[2], double* pb) {
+                                              double (&ub)[2], double* mu) {
     const double a = p[0], b = p[1], c = p[2], dd = p[3];
     const double x = y[0], w = y[1];
-    ub[0] = Ops::add(Ops::mul(Ops::sub(a, Ops::mul(b, w)), v[0]), Ops::mul(Ops::mul(c, w), v[1]));
-    ub[1] = Ops::add(Ops::mul(-Ops::mul(b, x), v[0]), Ops::mul(Ops::sub(Ops::mul(c, x), dd), v[1]));
-    const double xw = Ops::mul(x, w);
-    pb[0] = Ops::mul(x, v[0]);
-    pb[1] = -Ops::mul(xw, v[0]);
-    pb[2] = Ops::mul(xw, v[1]);
-    pb[3] = -Ops::mul(w, v[1]);
+    ub[0] = __fma_rn(__dmul_rn(c, w), v[1], __dmul_rn(__fma_rn(-b, w, a), v[0]));
+    ub[1] = __fma_rn(__fma_rn(c, x, -dd), v[1], __dmul_rn(-__dmul_rn(b, x), v[0]));
+    const double xw = __dmul_rn(x, w);
+    mu[0] = __fma_rn(x, v[0], mu[0]);
+    mu[1] = __fma_rn(-xw, v[0], mu[1]);
+    mu[2] = __fma_rn(xw, v[1], mu[2]);
+    mu[3] = __fma_rn(-w, v[1], mu[3]);
   }
 };
 

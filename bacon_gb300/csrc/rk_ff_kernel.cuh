@@ -42,8 +42,8 @@ __device__ __forceinline__ float log2_ratio(double num, double den) {
 // repeat the same rejected attempt until max_attempts.
 constexpr float kRejectMaxFactor = 0.99999905f;
 
-template <class Tab, class Rhs>
-__global__ void __launch_bounds__(256) rk_persistent_ff_kernel(const RkArgs a) {
+template <class Tab, class Rhs, int kMinBlocks = 1>
+__global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_ff_kernel(const RkArgs a) {
   constexpr int D = Rhs::DIM;
   constexpr int S = Tab::S;
   constexpr int P = Rhs::NP > 0 ? Rhs::NP : 1;

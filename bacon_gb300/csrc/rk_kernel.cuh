@@ -94,8 +94,12 @@ __device__ __forceinline__ void poison_components(double (&v)[D], uint32_t mask)
   }
 }
 
-template <class Tab, class Rhs, class Ops, bool kRecord = false>
-__global__ void __launch_bounds__(256) rk_persistent_kernel(const RkArgs a) {
+// kMinBlocks sets the register budget through the launch bounds: the compiler
+// keeps every thread within 65536 / (256 * kMinBlocks) registers (1: up to
+// 255, 3: 80, 4: 64), trading spills for resident warps.  The autotuner times
+// the budgets on the caller's batch.
+template <class Tab, class Rhs, class Ops, bool kRecord = false, int kMinBlocks = 1>
+__global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_kernel(const RkArgs a) {
   constexpr int D = Rhs::DIM;
   constexpr int S = Tab::S;
   constexpr int P = Rhs::NP > 0 ? Rhs::NP : 1;

@@ -329,10 +329,12 @@ def rk_solve_adjoint(y0, params, t0, t_end, target, *, rhs, tol, dt_min, dt_max,
 
 def rk_autotune(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
                 precision=FP64_EXACT, max_attempts=0, ctx: Context | None = None, out=None,
-                schedule=0) -> tuple[int, int]:
-    """Time the candidate launch shapes on this batch and cache the fastest in
-    the context (used by later solves of the same kernel and batch size).
-    Returns (threads per block, persistent CTAs per SM)."""
+                schedule=0, details=False):
+    """Time the candidate kernel variants (register budgets) and launch shapes
+    on this batch and cache the fastest in the context (used by later solves
+    of the same kernel and batch size).  Returns (threads per block,
+    persistent CTAs per SM), or with details=True a dict of the whole
+    bacon_tune_result."""
     ctx = ctx or default_context()
     device = _is_device(y0)
     dim, n = int(y0.shape[0]), int(y0.shape[1])
@@ -342,10 +344,26 @@ def rk_autotune(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45,
     if out is None:
         out = alloc_outputs(dim, n, device)
     res = make_result(out)
-    bb, bs = ctypes.c_int32(), ctypes.c_int32()
-    check(_capi.load().bacon_rk_autotune(ctx.handle, ctypes.byref(prob), ctypes.byref(opts),
-                                         ctypes.byref(res), ctypes.byref(bb), ctypes.byref(bs)))
-    return bb.value, bs.value
+    t = _capi.TuneResult()
+    check(_capi.load().bacon_rk_autotune_ex(ctx.handle, ctypes.byref(prob), ctypes.byref(opts),
+                                            ctypes.byref(res), ctypes.byref(t)))
+    if details:
+        return {f: getattr(t, f) for f, _ in _capi.TuneResult._fields_}
+    return t.block, t.blocks_per_sm
+
+
+def rk_set_tuned(y0, *, rhs, variant, block, blocks_per_sm, method=RK45, layout=FEHLBERG, precision=FP64_EXACT,
+                 ctx: Context | None = None):
+    """Pin the kernel variant and launch shape the context uses for this
+    kernel and batch size (bacon_rk_set_tuned)."""
+    ctx = ctx or default_context()
+    dim, n = int(y0.shape[0]), int(y0.shape[1])
+    prob = _capi.Problem()
+    prob.n, prob.dim, prob.rhs = n, dim, int(rhs)
+    opts = rk_options(method, layout, precision)
+    t = _capi.TuneResult()
+    t.variant, t.block, t.blocks_per_sm = int(variant), int(block), int(blocks_per_sm)
+    check(_capi.load().bacon_rk_set_tuned(ctx.handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(t)))
 
 
 BDF6, BDF2 = 0, 1

@@ -471,9 +471,9 @@ def main():
     # the fastest in the context; the timed solves below use it.
     cfg_line = config(args, b)
     if not args.skip_tune:
-        bb, bs = E.rk_autotune(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
-                               layout=E.FEHLBERG, precision=prec, ctx=ctx, out=out)
-        cfg_line["launch_shape"] = {"autotuned": True, "block": bb, "blocks_per_sm": bs}
+        tuned = E.rk_autotune(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                              layout=E.FEHLBERG, precision=prec, ctx=ctx, out=out, details=True)
+        cfg_line["launch_shape"] = {"autotuned": True, **tuned}
     for _ in range(max(args.warmup, 0)):
         solve()
     torch.cuda.synchronize()

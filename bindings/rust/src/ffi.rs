@@ -119,6 +119,19 @@ pub struct bacon_ragged_result {
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug)]
+pub struct bacon_tune_result {
+    pub variant: i32,
+    pub max_registers: i32,
+    pub systems_per_warp: i32,
+    pub block: i32,
+    pub blocks_per_sm: i32,
+    pub candidates: i32,
+    pub best_ms: f64,
+    pub default_ms: f64,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
 pub struct bacon_dense_output {
     pub capacity: i64,
     pub t: *mut f64,
@@ -159,6 +172,19 @@ extern "C" {
         result: *mut bacon_rk_result,
         best_block: *mut i32,
         best_blocks_per_sm: *mut i32,
+    ) -> c_int;
+    pub fn bacon_rk_autotune_ex(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_rk_options,
+        result: *mut bacon_rk_result,
+        tuned: *mut bacon_tune_result,
+    ) -> c_int;
+    pub fn bacon_rk_set_tuned(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_rk_options,
+        tuned: *const bacon_tune_result,
     ) -> c_int;
     pub fn bacon_rk_solve_plain(
         ctx: *mut bacon_ctx,

@@ -213,6 +213,36 @@ int bacon_rk_autotune(bacon_ctx* ctx, const bacon_problem* problem,
                       const bacon_rk_options* options, bacon_rk_result* result,
                       int32_t* best_block, int32_t* best_blocks_per_sm);
 
+/* What the autotuner chose for a batch, and what it measured.  The
+ * persistent kernels keep one system per lane (32 systems per warp): the
+ * FP64 pipe charges a warp instruction the same time however few lanes are
+ * active, so splitting a system across lanes multiplies its FP64 time.  The
+ * choices are the register budget (kernel variant) and the launch shape. */
+typedef struct {
+  int32_t variant;          /* 0: default kernel; 1, 2: register-capped variants */
+  int32_t max_registers;    /* the variant's budget per thread, 0 = the compiler's */
+  int32_t systems_per_warp; /* 32 */
+  int32_t block;            /* threads per block */
+  int32_t blocks_per_sm;    /* persistent CTAs per SM */
+  int32_t candidates;       /* (variant, shape) pairs timed */
+  double best_ms;           /* integration-kernel time of the choice */
+  double default_ms;        /* same without tuning (occupancy model, variant 0) */
+} bacon_tune_result;
+
+/* bacon_rk_autotune over register budgets as well as launch shapes: times
+ * the default kernel and, where compiled (RKF45 fehlberg reading, Van der
+ * Pol / Lorenz-63 / Lotka-Volterra, FP64_EXACT and FP32_COMP), the variants
+ * capped at 80 and 64 registers per thread, each at several shapes, and
+ * caches the fastest (variant, shape) in the context for this kernel and
+ * batch size.  Results of every variant are bit-identical. */
+int bacon_rk_autotune_ex(bacon_ctx* ctx, const bacon_problem* problem, const bacon_rk_options* options,
+                         bacon_rk_result* result, bacon_tune_result* tuned);
+/* Stores a tuning (variant, block, blocks_per_sm of `tuned`) in the context's
+ * cache for this kernel and batch size, as the autotuner would: a choice
+ * kept from an earlier run applies without timing again. */
+int bacon_rk_set_tuned(bacon_ctx* ctx, const bacon_problem* problem, const bacon_rk_options* options,
+                       const bacon_tune_result* tuned);
+
 /* The same solve with the plain one-launch-per-attempt GPU baseline (state,
  * t and dt in HBM, host loop until every system is done).  Same results. */
 int bacon_rk_solve_plain(bacon_ctx* ctx, const bacon_problem* problem,

@@ -26,9 +26,11 @@
 #define ORC_MAX_P 16
 
 /* ---- right-hand-side derivatives ---------------------------------------- */
-/* ubar = J(y)^T v and pbar = (df/dp)(y)^T v, evaluated in a fixed order. */
+/* ubar = J(y)^T v, and mu += (df/dp)(y)^T v: the adjoint's own arithmetic,
+ * fused multiply-adds (C's fma, one rounding each) in the order the CUDA
+ * reverse kernel executes (Vjp<> in bacon_gb300/csrc/rhs.cuh). */
 static int rhs_vjp(int32_t rhs, int32_t dim, const double* y, const double* p, const double* v,
-                   double* ubar, double* pbar) {
+                   double* ubar, double* mu) {
   switch (rhs) {
     case ORC_RHS_EXP:
       for (int d = 0; d < dim; ++d) ubar[d] = v[d];
@@ -41,33 +43,33 @@ static int rhs_vjp(int32_t rhs, int32_t dim, const double* y, const double* p, c
       ubar[1] = v[0];
       return 0;
     case ORC_RHS_VDP: {
-      const double mu = p[0], y0 = y[0], y1 = y[1];
-      const double w = 1.0 - (y0 * y0);
-      ubar[0] = ((((-2.0 * mu) * y0) * y1) - 1.0) * v[1];
-      ubar[1] = v[0] + ((mu * w) * v[1]);
-      pbar[0] = (w * y1) * v[1];
+      const double m = p[0], y0 = y[0], y1 = y[1];
+      const double w = fma(-y0, y0, 1.0);
+      ubar[0] = fma((-2.0 * m) * y0, y1, -1.0) * v[1];
+      ubar[1] = fma(m * w, v[1], v[0]);
+      mu[0] = fma(w * y1, v[1], mu[0]);
       return 0;
     }
     case ORC_RHS_LORENZ: {
       const double s = p[0], r = p[1], b = p[2];
-      ubar[0] = (((-s) * v[0]) + ((r - y[2]) * v[1])) + (y[1] * v[2]);
-      ubar[1] = ((s * v[0]) - v[1]) + (y[0] * v[2]);
-      ubar[2] = ((-y[0]) * v[1]) - (b * v[2]);
-      pbar[0] = (y[1] - y[0]) * v[0];
-      pbar[1] = y[0] * v[1];
-      pbar[2] = -(y[2] * v[2]);
+      ubar[0] = fma(y[1], v[2], fma(r - y[2], v[1], (-s) * v[0]));
+      ubar[1] = fma(y[0], v[2], fma(s, v[0], -v[1]));
+      ubar[2] = fma(-y[0], v[1], -(b * v[2]));
+      mu[0] = fma(y[1] - y[0], v[0], mu[0]);
+      mu[1] = fma(y[0], v[1], mu[1]);
+      mu[2] = fma(-y[2], v[2], mu[2]);
       return 0;
     }
     case ORC_RHS_LOTKA: {
       const double a = p[0], b = p[1], c = p[2], dd = p[3];
       const double x = y[0], w = y[1];
-      ubar[0] = ((a - (b * w)) * v[0]) + ((c * w) * v[1]);
-      ubar[1] = ((-(b * x)) * v[0]) + (((c * x) - dd) * v[1]);
+      ubar[0] = fma(c * w, v[1], fma(-b, w, a) * v[0]);
+      ubar[1] = fma(fma(c, x, -dd), v[1], (-(b * x)) * v[0]);
       const double xw = x * w;
-      pbar[0] = x * v[0];
-      pbar[1] = -(xw * v[0]);
-      pbar[2] = xw * v[1];
-      pbar[3] = -(w * v[1]);
+      mu[0] = fma(x, v[0], mu[0]);
+      mu[1] = fma(-xw, v[0], mu[1]);
+      mu[2] = fma(xw, v[1], mu[2]);
+      mu[3] = fma(-w, v[1], mu[3]);
       return 0;
     }
     default:
@@ -118,16 +120,18 @@ static int rhs_jvp(int32_t rhs, int32_t dim, const double* y, const double* p, c
 /* ---- one step of the RK map with a frozen dt ----------------------------- */
 /* Same operations as an accepted attempt of the forward solve, zero
  * coefficients skipped (they only matter for non-finite stage values).
- * Stage inputs are returned in Y[i][d]. */
-static void step_map(const orc_tableau* tb, int32_t rhs, int32_t dim, const double* p, double t,
-                     double dt, const double* y, double* y_next,
-                     double Y[ORC_MAX_STAGES][ORC_MAX_DIM], double K[ORC_MAX_STAGES][ORC_MAX_DIM]) {
+ * fused = 1 contracts every "v += K * c" into one fused multiply-add, as the
+ * CUDA reverse kernel's replay does.  Stage inputs are returned in Y[i][d]. */
+static void step_map_x(const orc_tableau* tb, int32_t rhs, int32_t dim, const double* p, double t,
+                       double dt, const double* y, double* y_next,
+                       double Y[ORC_MAX_STAGES][ORC_MAX_DIM], double K[ORC_MAX_STAGES][ORC_MAX_DIM], int fused) {
   double f[ORC_MAX_DIM];
   for (int i = 0; i < tb->s; ++i) {
     for (int d = 0; d < dim; ++d) Y[i][d] = y[d];
     for (int j = 0; j < tb->s; ++j) {
       if (tb->m[i][j] == 0.0) continue;
-      for (int d = 0; d < dim; ++d) Y[i][d] = Y[i][d] + (K[j][d] * tb->m[i][j]);
+      for (int d = 0; d < dim; ++d)
+        Y[i][d] = fused ? fma(K[j][d], tb->m[i][j], Y[i][d]) : Y[i][d] + (K[j][d] * tb->m[i][j]);
     }
     const double st = t + (tb->c[i] * dt);
     oracle_rhs(rhs, dim, st, Y[i], p, NULL, f);
@@ -136,8 +140,15 @@ static void step_map(const orc_tableau* tb, int32_t rhs, int32_t dim, const doub
   for (int d = 0; d < dim; ++d) y_next[d] = y[d];
   for (int j = 0; j < tb->s; ++j) {
     if (tb->b[j] == 0.0) continue;
-    for (int d = 0; d < dim; ++d) y_next[d] = y_next[d] + (K[j][d] * tb->b[j]);
+    for (int d = 0; d < dim; ++d)
+      y_next[d] = fused ? fma(K[j][d], tb->b[j], y_next[d]) : y_next[d] + (K[j][d] * tb->b[j]);
   }
+}
+
+static void step_map(const orc_tableau* tb, int32_t rhs, int32_t dim, const double* p, double t,
+                     double dt, const double* y, double* y_next,
+                     double Y[ORC_MAX_STAGES][ORC_MAX_DIM], double K[ORC_MAX_STAGES][ORC_MAX_DIM]) {
+  step_map_x(tb, rhs, dim, p, t, dt, y, y_next, Y, K, 0);
 }
 
 static double loss_of(const double* y, const double* target, int32_t dim) {
@@ -184,7 +195,9 @@ int32_t oracle_rk_adjoint_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim
                               int32_t n_params, const double* p, double t0,
                               double t_end, const double* y0,
                               const double* target, double* loss,
-                              double* dl_dy0, double* dl_dp) {
+                              double* dl_dy0, double* dl_dp, int32_t checkpoint_every) {
+  const int E = checkpoint_every > 0 ? checkpoint_every : 32;
+  if (E > 32) return -1;
   if (cfg->layout == ORC_LAYOUT_AS_COMPILED || dim > ORC_MAX_DIM || n_params > ORC_MAX_P) return -1;
   orc_tableau tb;
   orc_tableau_build(cfg->method, cfg->layout, &tb);
@@ -202,27 +215,43 @@ int32_t oracle_rk_adjoint_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim
   for (int d = 0; d < dim; ++d) lam[d] = 2.0 * (lg.yT[d] - target[d]);
   for (int k = 0; k < n_params; ++k) mu[k] = 0.0;
 
+  /* Segments of E accepted steps, last first: replay the segment from its
+   * checkpoint (the forward pass's own state at the segment start) with the
+   * fused step map, keeping every step's stage inputs, then sweep it in
+   * reverse. */
+  static __thread double Yseg[32][ORC_MAX_STAGES][ORC_MAX_DIM];
   double Y[ORC_MAX_STAGES][ORC_MAX_DIM], K[ORC_MAX_STAGES][ORC_MAX_DIM];
   double Kb[ORC_MAX_STAGES][ORC_MAX_DIM], yb[ORC_MAX_DIM], v[ORC_MAX_DIM], ub[ORC_MAX_DIM];
-  double pb[ORC_MAX_P], ynext[ORC_MAX_DIM];
-  for (int64_t n = lg.n - 1; n >= 0; --n) {
+  double ycur[ORC_MAX_DIM], ynext[ORC_MAX_DIM];
+  for (int64_t seg = (lg.n + E - 1) / E - 1; seg >= 0; --seg) {
+    const int64_t k0 = seg * E;
+    const int64_t m = (lg.n - k0) < E ? (lg.n - k0) : E;
+    memcpy(ycur, lg.y + (size_t)k0 * dim, sizeof(double) * dim);
+    double tcur = lg.t[k0];
+    for (int64_t j = 0; j < m; ++j) {
+      memset(K, 0, sizeof(K));
+      step_map_x(&tb, rhs, dim, p, tcur, lg.dt[k0 + j], ycur, ynext, Yseg[j], K, 1);
+      memcpy(ycur, ynext, sizeof(double) * dim);
+      tcur = tcur + lg.dt[k0 + j];
+    }
+    for (int64_t j = m - 1; j >= 0; --j) {
+    const int64_t n = k0 + j;
     const double dt = lg.dt[n];
-    memset(K, 0, sizeof(K));
-    step_map(&tb, rhs, dim, p, lg.t[n], dt, lg.y + (size_t)n * dim, ynext, Y, K);
+    memcpy(Y, Yseg[j], sizeof(Y));
     for (int i = 0; i < tb.s; ++i)
       for (int d = 0; d < dim; ++d) Kb[i][d] = lam[d] * tb.b[i];
     for (int d = 0; d < dim; ++d) yb[d] = lam[d];
     for (int i = tb.s - 1; i >= 0; --i) {
       for (int d = 0; d < dim; ++d) v[d] = Kb[i][d] * dt;
-      rhs_vjp(rhs, dim, Y[i], p, v, ub, pb);
-      for (int k = 0; k < n_params; ++k) mu[k] = mu[k] + pb[k];
+      rhs_vjp(rhs, dim, Y[i], p, v, ub, mu);
       for (int d = 0; d < dim; ++d) yb[d] = yb[d] + ub[d];
       for (int j = 0; j < i; ++j) {
         if (tb.m[i][j] == 0.0) continue;
-        for (int d = 0; d < dim; ++d) Kb[j][d] = Kb[j][d] + (ub[d] * tb.m[i][j]);
+        for (int d = 0; d < dim; ++d) Kb[j][d] = fma(ub[d], tb.m[i][j], Kb[j][d]);
       }
     }
     for (int d = 0; d < dim; ++d) lam[d] = yb[d];
+    }
   }
   for (int d = 0; d < dim; ++d) dl_dy0[d] = lam[d];
   for (int k = 0; k < n_params; ++k) dl_dp[k] = mu[k];

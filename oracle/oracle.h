@@ -193,7 +193,7 @@ int32_t oracle_rk_adjoint_one(const oracle_rk_cfg* cfg, int32_t rhs, int32_t dim
                               int32_t n_params, const double* p, double t0,
                               double t_end, const double* y0,
                               const double* target, double* loss,
-                              double* dl_dy0, double* dl_dp);
+                              double* dl_dy0, double* dl_dp, int32_t checkpoint_every);
 
 /* Forward (tangent-linear) sensitivities of the same loss through the same
  * frozen step sequence; agrees with the adjoint up to rounding. */

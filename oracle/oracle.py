@@ -125,7 +125,7 @@ def lib():
             L.oracle_rk_adjoint_one.restype = ctypes.c_int32
             L.oracle_rk_adjoint_one.argtypes = [
                 ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
-                ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp]
+                ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp, ctypes.c_int32]
             L.oracle_rk_fwdsens_one.restype = ctypes.c_int32
             L.oracle_rk_fwdsens_one.argtypes = [
                 ctypes.POINTER(_RkCfg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
@@ -239,8 +239,10 @@ def rhs_eval(rhs, t, y, params=None, shared=None):
     return f
 
 
-def rk_adjoint_one(cfg, rhs, y0, params, t0, t_end, target):
-    """Discrete adjoint (oracle): returns (status, loss, dL/dy0, dL/dp)."""
+def rk_adjoint_one(cfg, rhs, y0, params, t0, t_end, target, checkpoint_every=32):
+    """Discrete adjoint (oracle), segments of checkpoint_every accepted steps
+    replayed with fused multiply-adds as the GPU's reverse kernel does:
+    returns (status, loss, dL/dy0, dL/dp)."""
     L = lib()
     y0 = np.ascontiguousarray(y0, dtype=np.float64)
     p = np.ascontiguousarray(params, dtype=np.float64)
@@ -249,7 +251,7 @@ def rk_adjoint_one(cfg, rhs, y0, params, t0, t_end, target):
     gp = np.zeros(p.shape[0])
     loss = ctypes.c_double()
     st = L.oracle_rk_adjoint_one(ctypes.byref(cfg), rhs, y0.shape[0], p.shape[0], _dp(p), t0, t_end,
-                                 _dp(y0), _dp(tg), ctypes.byref(loss), _dp(gy), _dp(gp))
+                                 _dp(y0), _dp(tg), ctypes.byref(loss), _dp(gy), _dp(gp), int(checkpoint_every))
     return st, loss.value, gy, gp
 
 

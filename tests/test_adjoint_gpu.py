@@ -22,7 +22,8 @@ def test_lotka_volterra_adjoint_bit_exact(engine, oracle, every):
     assert sol.code == 0
     cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
     for i in range(0, b.n, 17):
-        st, L, gy, gp = oracle.rk_adjoint_one(cfg, b.rhs, b.y0[:, i], b.params[:, i], 0.0, 15.0, tg[:, i])
+        st, L, gy, gp = oracle.rk_adjoint_one(cfg, b.rhs, b.y0[:, i], b.params[:, i], 0.0, 15.0, tg[:, i],
+                                              checkpoint_every=every)
         assert st == 0
         assert sol.loss[i] == L
         np.testing.assert_array_equal(sol.dl_dy0[:, i], gy)

@@ -17,3 +17,28 @@ def test_autotune_caches_and_keeps_results(engine):
     after = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
     np.testing.assert_array_equal(after.y, before.y)
     np.testing.assert_array_equal(after.accepted, before.accepted)
+
+
+def test_autotune_register_budget_variants_identical(engine):
+    """The tuner times the register-capped variants too; whichever it
+    caches, the solve stays bit-identical."""
+    b = W.lorenz(n=1 << 20).subset(np.arange(0, 1 << 20, 64))  # 16384 systems
+    kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
+    before = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
+    t = engine.rk_autotune(b.y0, b.params, b.t0, b.t_end, details=True, **kw)
+    assert t["candidates"] == 8 + 2 * 4
+    assert t["variant"] in (0, 1, 2) and t["max_registers"] in (0, 80, 64)
+    assert t["best_ms"] <= t["default_ms"] * 1.05
+    after = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
+    np.testing.assert_array_equal(after.y, before.y)
+    np.testing.assert_array_equal(after.accepted, before.accepted)
+    for precision in (0, 2):
+        ctx = engine.Context(0)
+        ref = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, precision=precision, ctx=ctx, **kw)
+        for v, (blk, bps) in ((1, (256, 3)), (2, (256, 4))):
+            engine.rk_set_tuned(b.y0, rhs=b.rhs, variant=v, block=blk, blocks_per_sm=bps, precision=precision,
+                                ctx=ctx)
+            out = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, precision=precision, ctx=ctx, **kw)
+            np.testing.assert_array_equal(out.y, ref.y)
+            np.testing.assert_array_equal(out.rejected, ref.rejected)
+        ctx.close()
