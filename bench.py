@@ -338,8 +338,7 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
     # corrector, src/ivp/adams.rs): it restarts from an RK4 bootstrap after
     # every dt change, so it takes ~10^5..10^6 step calls per system.
     akw = dict(rhs=vb.rhs, tol=vb.tol, dt_min=vb.dt_min, dt_max=vb.dt_max, order=5, ctx=ctx)
-    E.adams_solve(vy, vp, 0.0, 10.0, **akw)
-    a5 = E.adams_solve(vy, vp, 0.0, 10.0, **akw)
+    a5 = E.adams_solve(vy, vp, 0.0, 10.0, **akw)  # ~20 s: no separate warm-up
     ams = ctx.last_kernel_ms()
     st = a5.status.cpu().numpy()
     out["adams5_van_der_pol_4096"] = {
@@ -350,6 +349,21 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
         "final_state_error_vs_rtol1e-12": ok_error(a5.y.cpu().numpy(), vref, st),
         "note": "status 8 = MinimumTimeDeltaExceeded, as the reference's Adams5 ends on these systems (bit-identical "
                 "to the CPU restatement); the launch lasts as long as the slowest system"}
+
+    # A batch that fills the GPU: 65,536 Van der Pol systems of the same
+    # distribution.  The launch still lasts as long as its slowest system, but
+    # 16x the systems share that time.
+    wb = W.van_der_pol(n=65536, seed=1)
+    wy, wp = to_dev(wb.y0, wb.params)
+    w5 = E.adams_solve(wy, wp, 0.0, 10.0, **dict(akw, tol=wb.tol, dt_min=wb.dt_min, dt_max=wb.dt_max))
+    wms = ctx.last_kernel_ms()
+    wst = w5.status.cpu().numpy()
+    out["adams5_van_der_pol_65536"] = {
+        "value": wb.n / (wms * 1e-3), "unit": "solves/s", "kernel_ms": wms,
+        "status_counts": {int(k): int((wst == k).sum()) for k in np.unique(wst)},
+        "step_calls_max": float((w5.accepted.double() + w5.rejected.double()).max().item()),
+        "what": "GPU-filling batch beside the 4096-system workload: the same generator and distributions, 16x the "
+                "systems"}
 
     # Linear y' = A y, shared A (n = 256), 65,536 states, tol 1e-8.
     lb = W.linear_shared()
@@ -581,14 +595,19 @@ def main():
         speedup_plain = value / world / plain_value
         extras["speedup_vs_plain"] = speedup_plain
 
-        # FP32-stage mode (float-float stages, FP64 control), same workload.
+        # FP32-stage mode (float-float stages, FP64 control), same workload,
+        # with its own autotuned kernel variant and launch shape.
         cout = E.alloc_outputs(3, b.n, device=True)
+        comp_tune = None
+        if not args.skip_tune:
+            comp_tune = E.rk_autotune(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                                      layout=E.FEHLBERG, precision=E.FP32_COMP, ctx=ctx, out=cout, details=True)
         solve(E.FP32_COMP, cout)
         comp_ms = event_timed(torch, ext, lambda: solve(E.FP32_COMP, cout), 3, flush)
         comp_value = b.n / (statistics.median(comp_ms) * 1e-3)
         extras["fp32_comp_mode"] = {"value": comp_value, "unit": UNIT,
                                     "speedup_vs_fp64_exact": comp_value / (value / world),
-                                    "speedup_vs_plain": comp_value / plain_value,
+                                    "speedup_vs_plain": comp_value / plain_value, "autotuned": comp_tune,
                                     "what": "float-float stages on the FP32 pipe, FP64 accept test and dt"}
 
         # The reference's literal tableau read row by row (1859/4014 kept):
@@ -774,6 +793,8 @@ def compact_summary(line):
         "linear_tc": {"solves_s": r3(g("linear_shared_A_256", "tensor_split", "value")),
                       "frac_bf16": r3(g("linear_shared_A_256", "tensor_split", "roofline", "frac"))},
         "vdp_solves_s": r3(g("van_der_pol_4096", "value")), "adams5_solves_s": r3(g("adams5_van_der_pol_4096", "value")),
+        "adams5_65536_solves_s": r3(g("adams5_van_der_pol_65536", "value")),
+        "adams5_cpu_16core_solves_s": r3(g("adams5_van_der_pol_4096", "cpu_baseline", "value")),
         "final_state_rel_max_vs_rtol1e-12": {
             "lorenz_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp64_exact", "rel_max")),
             "lorenz_fp32comp_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp32_comp", "rel_max")),
