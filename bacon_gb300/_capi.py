@@ -183,6 +183,8 @@ SIGNATURES = {
     "bacon_ctx_set_fault_injection": (ctypes.c_int, [_VP, ctypes.c_int]),
     "bacon_rk_solve": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                       ctypes.POINTER(RkResult)]),
+    "bacon_rk_solve_user": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
+                                           ctypes.POINTER(RkResult), ctypes.c_void_p, ctypes.c_void_p]),
     "bacon_rk_solve_plain": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                             ctypes.POINTER(RkResult)]),
     "bacon_rk_validate": (ctypes.c_int, [ctypes.POINTER(Problem)]),

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -269,7 +270,7 @@ int bacon_rk_validate(const bacon_problem* p) {
   if (!p->t0 && !p->t_end && p->t0_scalar >= p->t_end_scalar)
     return fail(BACON_TIME_END_OOB, "ending time is not after the initial time");
   const int ed = expected_dim(p->rhs);
-  if (p->rhs < 0 || p->rhs > BACON_RHS_LINEAR) return fail(BACON_INVALID_ARGUMENT, "unknown rhs");
+  if (p->rhs < 0 || p->rhs > BACON_RHS_USER) return fail(BACON_INVALID_ARGUMENT, "unknown rhs");
   if (ed > 0 && p->dim != ed) return fail(BACON_INVALID_ARGUMENT, "dim does not match the rhs");
   if (p->n_params < expected_params(p->rhs, p->dim))
     return fail(BACON_INVALID_ARGUMENT, "too few parameters for the rhs");
@@ -786,6 +787,93 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   } else {
     if ((rc = enqueue_all()) != BACON_OK) return rc;
   }
+  c->launches += lpt ? 5 : 1;
+  c->ev_valid = true;
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  BACON_CUDA(cudaGetLastError());
+  return batch_return_code(c, r, host, o);
+}
+
+// The caller's right-hand side: the engine's staging, order and result
+// handling around a kernel the caller compiled (include/bacon_gb300_rhs.cuh).
+static_assert(sizeof(bacon_rk_kernel_args) == sizeof(bacon::RkArgs), "kernel argument block layout");
+static_assert(offsetof(bacon_rk_kernel_args, traj_off) == offsetof(bacon::RkArgs, traj_off), "layout");
+static_assert(offsetof(bacon_rk_kernel_args, order) == offsetof(bacon::RkArgs, order), "layout");
+static_assert(offsetof(bacon_rk_kernel_args, ckpt_slots) == offsetof(bacon::RkArgs, ckpt_slots), "layout");
+
+extern "C" int bacon_rk_solve_user(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
+                                   bacon_rk_result* r, bacon_rk_launch_fn launch, void* user) {
+  NvtxRange nvtx_range("bacon_rk_solve_user");
+  if (!c || !opt || !launch) return fail(BACON_INVALID_ARGUMENT, "NULL context, options or launcher");
+  int rc = bacon_rk_validate(p);
+  if (rc != BACON_OK) return rc;
+  if (p->rhs != BACON_RHS_USER) return fail(BACON_INVALID_ARGUMENT, "bacon_rk_solve_user takes BACON_RHS_USER");
+  if ((rc = check_result_ptrs(p, r)) != BACON_OK) return rc;
+  if (opt->method != BACON_RK45 && opt->method != BACON_RK23) return fail(BACON_INVALID_ARGUMENT, "unknown method");
+  if (opt->layout < 0 || opt->layout > 2) return fail(BACON_INVALID_ARGUMENT, "unknown layout");
+  if (opt->precision < 0 || opt->precision > 2) return fail(BACON_INVALID_ARGUMENT, "unknown precision");
+  if (p->n == 0) return BACON_OK;
+  BACON_CUDA(cudaSetDevice(c->device));
+  const bool host = opt->memory == BACON_MEM_HOST;
+  Resolved o{};
+  if ((rc = stage_inputs(c, p, r, host, o)) != BACON_OK) return rc;
+  double dt_min = p->dt_min;
+  clamp_dt(dt_min, p->dt_max);
+  bacon::RkArgs a{};
+  a.n = p->n;
+  a.y0 = o.y0;
+  a.params = o.params;
+  a.t0 = o.t0;
+  a.t_end = o.t_end;
+  a.t0_s = p->t0_scalar;
+  a.t_end_s = p->t_end_scalar;
+  a.tol = p->tol;
+  a.dt_min = dt_min;
+  a.dt_max = p->dt_max;
+  a.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  a.y_out = o.y_out;
+  a.t_out = o.t_out;
+  a.accepted = o.acc;
+  a.rejected = o.rej;
+  a.status = o.st;
+  a.traj_t = o.traj_t;
+  a.traj_y = o.traj_y;
+  a.traj_cap = (o.traj_t ? r->traj_cap : 0);
+  a.queue = c->d_ctl;
+  a.first_fail = c->d_ctl + 1;
+  const bool per_system_times = (p->t0 != nullptr) || (p->t_end != nullptr);
+  const bool lpt = (opt->schedule == 2 || (opt->schedule == 0 && per_system_times)) && p->n < (1ll << 32);
+  bacon::OrderArgs oa{};
+  if (lpt) {
+    BACON_CUDA(c->ord.ensure(static_cast<size_t>(p->n) * sizeof(uint32_t)));
+    BACON_CUDA(c->ord_scratch.ensure(sizeof(bacon::OrderScratch)));
+    oa = bacon::OrderArgs{p->n, o.t0, o.t_end, p->t0_scalar, p->t_end_scalar,
+                          c->ord_scratch.as<bacon::OrderScratch>(), c->ord.as<uint32_t>()};
+    a.order = oa.order;
+  }
+  const int block = opt->block > 0 ? opt->block : 128;
+  if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
+  const int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 2;
+  long long grid = static_cast<long long>(c->num_sms) * bps;
+  const long long need = (p->n + block - 1) / block;
+  if (grid > need) grid = need;
+  if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
+  if (lpt) BACON_CUDA(bacon::enqueue_lpt_order(oa, c->num_sms, c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaMemsetAsync(c->d_ctl + 1, 0xff, sizeof(unsigned long long), c->stream));
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  bacon_rk_kernel_args ka;
+  std::memcpy(&ka, &a, sizeof(ka));
+  const int lrc = launch(&ka, opt->method, opt->layout, opt->precision, static_cast<int32_t>(grid), block,
+                         reinterpret_cast<void*>(c->stream), user);
+  if (lrc != BACON_OK) {
+    cudaStreamSynchronize(c->stream);
+    return fail(lrc, "the caller's launcher failed for this (method, layout, precision)");
+  }
+  BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
+  if (host && (rc = enqueue_d2h(c, p, r, o)) != BACON_OK) return rc;
+  BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 1, c->d_ctl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
   c->launches += lpt ? 5 : 1;
   c->ev_valid = true;
   BACON_CUDA(cudaStreamSynchronize(c->stream));

@@ -119,6 +119,39 @@ pub struct bacon_ragged_result {
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug)]
+pub struct bacon_rk_kernel_args {
+    pub n: i64,
+    pub y0: *const f64,
+    pub params: *const f64,
+    pub t0: *const f64,
+    pub t_end: *const f64,
+    pub t0_s: f64,
+    pub t_end_s: f64,
+    pub tol: f64,
+    pub dt_min: f64,
+    pub dt_max: f64,
+    pub max_attempts: i64,
+    pub y_out: *mut f64,
+    pub t_out: *mut f64,
+    pub accepted: *mut i32,
+    pub rejected: *mut i32,
+    pub status: *mut i32,
+    pub traj_t: *mut f64,
+    pub traj_y: *mut f64,
+    pub traj_cap: i32,
+    pub traj_off: *const i64,
+    pub queue: *mut u64,
+    pub first_fail: *mut u64,
+    pub order: *const u32,
+    pub dt_log: *mut f64,
+    pub ckpt: *mut f64,
+    pub ckpt_every: i32,
+    pub max_steps: i32,
+    pub ckpt_slots: i32,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
 pub struct bacon_tune_result {
     pub variant: i32,
     pub max_registers: i32,
@@ -185,6 +218,14 @@ extern "C" {
         problem: *const bacon_problem,
         options: *const bacon_rk_options,
         tuned: *const bacon_tune_result,
+    ) -> c_int;
+    pub fn bacon_rk_solve_user(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        options: *const bacon_rk_options,
+        result: *mut bacon_rk_result,
+        launch: bacon_rk_launch_fn,
+        user: *mut c_void,
     ) -> c_int;
     pub fn bacon_rk_solve_plain(
         ctx: *mut bacon_ctx,
@@ -275,3 +316,18 @@ extern "C" {
     pub fn bacon_builder_problem(b: *const bacon_builder, out: *mut bacon_problem) -> c_int;
     pub fn bacon_measure_fp64_peak(ctx: *mut bacon_ctx, gflops: *mut f64) -> c_int;
 }
+
+/// `bacon_rk_launch_fn`: the caller's launcher of its own right-hand side's
+/// persistent kernel (see include/bacon_gb300_rhs.cuh).
+pub type bacon_rk_launch_fn = Option<
+    unsafe extern "C" fn(
+        args: *const bacon_rk_kernel_args,
+        method: i32,
+        layout: i32,
+        precision: i32,
+        grid: i32,
+        block: i32,
+        stream: *mut c_void,
+        user: *mut c_void,
+    ) -> c_int,
+>;

@@ -70,7 +70,8 @@ typedef enum {
   BACON_RHS_LOTKA = 7,      /* Lotka-Volterra      dim 2,   (a,b,c,d)      */
   BACON_RHS_ROBERTSON = 8,  /* Robertson kinetics  dim 3,   (k1,k2,k3)     */
   BACON_RHS_CHAIN = 9,      /* spring-mass chain   dim 2n,  (k_0..k_{n-1}, c) */
-  BACON_RHS_LINEAR = 10     /* y' = A y, one shared dense A                */
+  BACON_RHS_LINEAR = 10,    /* y' = A y, one shared dense A                */
+  BACON_RHS_USER = 11       /* compiled by the caller: bacon_rk_solve_user */
 } bacon_rhs;
 
 /* ---- methods and variants ---------------------------------------------- */
@@ -248,6 +249,62 @@ int bacon_rk_set_tuned(bacon_ctx* ctx, const bacon_problem* problem, const bacon
 int bacon_rk_solve_plain(bacon_ctx* ctx, const bacon_problem* problem,
                          const bacon_rk_options* options,
                          bacon_rk_result* result);
+
+/* ---- right-hand sides compiled by the caller ------------------------------ */
+/* The reference's derivative is any Rust closure (src/ivp.rs:34-48).  The
+ * registry above covers the benchmark's systems; any other right-hand side
+ * is compiled by the caller into the same persistent kernel: a device functor
+ * (dimension, parameter count, eval) in a .cu file that includes
+ * include/bacon_gb300_rhs.cuh, which defines a launcher with
+ * BACON_DEFINE_RK_LAUNCHER.  The engine does everything around the launch
+ * (staging, longest-first order, counters, results, status) and calls the
+ * launcher on its stream with the kernel's arguments.
+ *
+ * bacon_rk_kernel_args is the persistent kernel's argument block, field for
+ * field (bacon_gb300/csrc/rk_kernel.cuh RkArgs); the launcher passes it on
+ * unchanged. */
+typedef struct {
+  int64_t n;
+  const double* y0;
+  const double* params;
+  const double* t0;
+  const double* t_end;
+  double t0_s, t_end_s;
+  double tol, dt_min, dt_max;
+  int64_t max_attempts;
+  double* y_out;
+  double* t_out;
+  int32_t* accepted;
+  int32_t* rejected;
+  int32_t* status;
+  double* traj_t;
+  double* traj_y;
+  int32_t traj_cap;
+  const int64_t* traj_off;
+  unsigned long long* queue;
+  unsigned long long* first_fail;
+  const uint32_t* order;
+  double* dt_log;
+  double* ckpt;
+  int32_t ckpt_every;
+  int32_t max_steps;
+  int32_t ckpt_slots;
+} bacon_rk_kernel_args;
+
+/* Launches the caller's kernel for (method, layout, precision) with `grid`
+ * CTAs of `block` threads on `stream` (a cudaStream_t).  Returns BACON_OK,
+ * BACON_UNSUPPORTED when that combination was not compiled, or
+ * BACON_CUDA_ERROR. */
+typedef int (*bacon_rk_launch_fn)(const bacon_rk_kernel_args* args, int32_t method, int32_t layout,
+                                  int32_t precision, int32_t grid, int32_t block, void* stream, void* user);
+
+/* bacon_rk_solve for problem->rhs == BACON_RHS_USER: problem->dim and
+ * n_params describe the caller's functor; its kernel runs through `launch`
+ * (`user` is passed through).  options->block / blocks_per_sm set the launch
+ * shape (0: 128 threads, 2 CTAs per SM).  Same results, statuses and
+ * trajectory slabs as bacon_rk_solve. */
+int bacon_rk_solve_user(bacon_ctx* ctx, const bacon_problem* problem, const bacon_rk_options* options,
+                        bacon_rk_result* result, bacon_rk_launch_fn launch, void* user);
 
 /* ---- BDF (src/ivp/bdf.rs) ------------------------------------------------ */
 typedef enum { BACON_BDF6 = 0, BACON_BDF2 = 1 } bacon_bdf_method;

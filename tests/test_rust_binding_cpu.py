@@ -16,8 +16,10 @@ HEADER = os.path.join(ROOT, "include", "bacon_gb300.h")
 FFI = os.path.join(ROOT, "bindings", "rust", "src", "ffi.rs")
 GPU = os.path.join(ROOT, "bindings", "rust", "src", "gpu.rs")
 
-C_SCALARS = {"int": "i32", "int32_t": "i32", "int64_t": "i64", "double": "f64", "void": "void", "char": "i8"}
-R_SCALARS = {"c_int": "i32", "i32": "i32", "i64": "i64", "f64": "f64", "c_void": "void", "c_char": "i8"}
+C_SCALARS = {"int": "i32", "int32_t": "i32", "int64_t": "i64", "double": "f64", "void": "void", "char": "i8",
+             "unsigned long long": "u64", "uint32_t": "u32"}
+R_SCALARS = {"c_int": "i32", "i32": "i32", "i64": "i64", "f64": "f64", "c_void": "void", "c_char": "i8",
+             "u64": "u64", "u32": "u32"}
 
 
 def _c_type(decl: str) -> str:
@@ -28,7 +30,7 @@ def _c_type(decl: str) -> str:
     const = words[0] == "const"
     if const:
         words = words[1:]
-    base = C_SCALARS.get(words[0], words[0])
+    base = C_SCALARS.get(" ".join(words), C_SCALARS.get(words[0], words[0]))
     if stars == 0:
         return base
     t = ("*const " if const else "*mut ") + base
@@ -77,7 +79,8 @@ def _header():
 
 def _rust():
     text = re.sub(r"//[^\n]*", "", open(FFI).read())
-    block = text[text.index('extern "C"'):]
+    block = text[text.index('extern "C" {'):]
+    block = block[:block.index("\n}\n") + 3]
     funcs = {}
     for name, args, ret in re.findall(r"pub fn (\w+)\s*\(([^)]*)\)\s*(?:->\s*([^;]+))?;", block, flags=re.S):
         params = []
