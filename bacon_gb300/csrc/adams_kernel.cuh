@@ -94,6 +94,10 @@ struct AdamsState {
   double pv_t[kCap], pv_y[kCap][D];
   double pd[kCap][D];
   int npv, npd, yield_memory;
+  // A step() call whose RK4 run is in progress: rk_left RK4 steps remain,
+  // rk_i is the next one's index, rk_kind 1 = the start-up run (the call
+  // returns Redo), 2 = the end-clamped single step (it yields an item).
+  int rk_left, rk_i, rk_kind;
 };
 
 template <int O, int D>
@@ -159,49 +163,59 @@ __device__ __forceinline__ void ad_pv_select(const AdamsState<O, D>& s, int i, d
   }
 }
 
-// AdamsSolver::runge_kutta (src/ivp/adams.rs:344-395).
+// AdamsSolver::runge_kutta (src/ivp/adams.rs:344-395), one RK4 step at a
+// time: step i of a run (the history pushes of the reference's loop happen
+// from i = 1 on), then, after the last, the closing evaluation and pushes.
+// A run of O - 1 steps costs ~20 right-hand-side evaluations against ~1 for a
+// PECE step, so the kernel advances a run by one RK4 step per loop iteration:
+// the lanes of a warp that are in a PECE step then wait for one RK4 step of
+// a neighbour, not for its whole run.  The operations and their order are the
+// reference's.
 template <int O, class Rhs>
-__device__ __forceinline__ void ad_runge_kutta(AdamsState<O, Rhs::DIM>& s, const double* p, int iterations) {
+__device__ __forceinline__ void ad_rk4_step(AdamsState<O, Rhs::DIM>& s, const double* p, int i) {
   using X = ExactOps;
   constexpr int D = Rhs::DIM;
   double k1[D], k2[D], k3[D], k4[D], it[D], f[D];
-  for (int i = 0; i < iterations; ++i) {
-    Rhs::template eval<X>(s.time, s.state, p, f);
-#pragma unroll
-    for (int d = 0; d < D; ++d) k1[d] = X::mul(f[d], s.dt);
-#pragma unroll
-    for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], X::mul(k1[d], 0.5));
-    Rhs::template eval<X>(X::add(s.time, X::mul(0.5, s.dt)), it, p, f);
-#pragma unroll
-    for (int d = 0; d < D; ++d) k2[d] = X::mul(f[d], s.dt);
-#pragma unroll
-    for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], X::mul(k2[d], 0.5));
-    Rhs::template eval<X>(X::add(s.time, X::mul(0.5, s.dt)), it, p, f);
-#pragma unroll
-    for (int d = 0; d < D; ++d) k3[d] = X::mul(f[d], s.dt);
-#pragma unroll
-    for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], k3[d]);
-    Rhs::template eval<X>(X::add(s.time, s.dt), it, p, f);
-#pragma unroll
-    for (int d = 0; d < D; ++d) k4[d] = X::mul(f[d], s.dt);
-    if (i != 0) {
-      Rhs::template eval<X>(s.time, s.state, p, f);
-      ad_pd_push(s, f);
-      ad_pv_push(s, s.time, s.state);
-    }
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      const double comb = X::add(X::add(X::add(k1[d], X::mul(k2[d], 2.0)), X::mul(k3[d], 2.0)), k4[d]);
-      s.state[d] = X::add(s.state[d], X::mul(comb, 1.0 / 6.0));
-    }
-    s.time = X::add(s.time, s.dt);
-  }
   Rhs::template eval<X>(s.time, s.state, p, f);
+#pragma unroll
+  for (int d = 0; d < D; ++d) k1[d] = X::mul(f[d], s.dt);
+#pragma unroll
+  for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], X::mul(k1[d], 0.5));
+  Rhs::template eval<X>(X::add(s.time, X::mul(0.5, s.dt)), it, p, f);
+#pragma unroll
+  for (int d = 0; d < D; ++d) k2[d] = X::mul(f[d], s.dt);
+#pragma unroll
+  for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], X::mul(k2[d], 0.5));
+  Rhs::template eval<X>(X::add(s.time, X::mul(0.5, s.dt)), it, p, f);
+#pragma unroll
+  for (int d = 0; d < D; ++d) k3[d] = X::mul(f[d], s.dt);
+#pragma unroll
+  for (int d = 0; d < D; ++d) it[d] = X::add(s.state[d], k3[d]);
+  Rhs::template eval<X>(X::add(s.time, s.dt), it, p, f);
+#pragma unroll
+  for (int d = 0; d < D; ++d) k4[d] = X::mul(f[d], s.dt);
+  if (i != 0) {
+    Rhs::template eval<X>(s.time, s.state, p, f);
+    ad_pd_push(s, f);
+    ad_pv_push(s, s.time, s.state);
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double comb = X::add(X::add(X::add(k1[d], X::mul(k2[d], 2.0)), X::mul(k3[d], 2.0)), k4[d]);
+    s.state[d] = X::add(s.state[d], X::mul(comb, 1.0 / 6.0));
+  }
+  s.time = X::add(s.time, s.dt);
+}
+
+template <int O, class Rhs>
+__device__ __forceinline__ void ad_rk4_close(AdamsState<O, Rhs::DIM>& s, const double* p) {
+  double f[Rhs::DIM];
+  Rhs::template eval<ExactOps>(s.time, s.state, p, f);
   ad_pd_push(s, f);
   ad_pv_push(s, s.time, s.state);
 }
 
-enum : int { kAdItem = 0, kAdRedo = 1, kAdDone = 2, kAdFail = 3 };
+enum : int { kAdItem = 0, kAdRedo = 1, kAdDone = 2, kAdFail = 3, kAdPending = 4 };
 
 // AdamsSolver::step (src/ivp/adams.rs:411-565).
 template <int O, class Rhs>
@@ -230,19 +244,19 @@ __device__ __forceinline__ int ad_step(AdamsState<O, Rhs::DIM>& s, const double*
   if (s.time >= s.end) return kAdDone;
   if (X::add(s.time, s.dt) >= s.end) {
     s.dt = X::sub(s.end, s.time);
-    ad_runge_kutta<O, Rhs>(s, p, 1);
-    double back_t;
-    ad_pv_select<AdamsState<O, D>::kCap>(s, s.npv - 1, back_t, iy);
-    it = s.time;
-    return kAdItem;
+    s.rk_kind = 2;  // one RK4 step, then yield the last history value
+    s.rk_i = 0;
+    s.rk_left = 1;
+    return kAdPending;
   }
   if (s.npv == 0) {
 #pragma unroll
     for (int d = 0; d < D; ++d) s.save[d] = s.state[d];
     if (X::add(s.time, X::mul(s.dt, order - 1.0)) >= s.end) s.dt = X::div(X::sub(s.end, s.time), order - 1.0);
-    ad_runge_kutta<O, Rhs>(s, p, O - 1);
-    s.yield_memory = O;
-    return kAdRedo;
+    s.rk_kind = 1;  // the start-up run of O - 1 RK4 steps, then Redo
+    s.rk_i = 0;
+    s.rk_left = O - 1;
+    return kAdPending;
   }
   double scratch[D], pred[D], corr[D], impl[D], diff[D];
 #pragma unroll
@@ -307,6 +321,28 @@ __device__ __forceinline__ int ad_step(AdamsState<O, Rhs::DIM>& s, const double*
   return kAdRedo;
 }
 
+// Advances a step() call's RK4 run by one step; when the run is complete,
+// finishes the call as the reference's step() does after runge_kutta
+// returns: Redo for the start-up run, the last history value for the
+// end-clamped step.
+template <int O, class Rhs>
+__device__ __forceinline__ int ad_continue(AdamsState<O, Rhs::DIM>& s, const double* p, double& it,
+                                           double (&iy)[Rhs::DIM]) {
+  ad_rk4_step<O, Rhs>(s, p, s.rk_i);
+  s.rk_i += 1;
+  s.rk_left -= 1;
+  if (s.rk_left > 0) return kAdPending;
+  ad_rk4_close<O, Rhs>(s, p);
+  if (s.rk_kind == 1) {
+    s.yield_memory = O;
+    return kAdRedo;
+  }
+  double back_t;
+  ad_pv_select<AdamsState<O, Rhs::DIM>::kCap>(s, s.npv - 1, back_t, iy);
+  it = s.time;
+  return kAdItem;
+}
+
 template <int O, class Rhs>
 __global__ void __launch_bounds__(128) adams_persistent_kernel(const AdamsArgs a) {
   constexpr int D = Rhs::DIM;
@@ -326,6 +362,7 @@ __global__ void __launch_bounds__(128) adams_persistent_kernel(const AdamsArgs a
     s.dt_max = a.dt_max;
     s.dt = ExactOps::mul(ExactOps::add(a.dt_max, a.dt_min), 0.5);
     s.npv = s.npd = s.yield_memory = 0;
+    s.rk_left = s.rk_i = s.rk_kind = 0;
     double last_y[D], last_t = s.time;
 #pragma unroll
     for (int d = 0; d < D; ++d) s.state[d] = last_y[d] = a.y0[d * n + idx];
@@ -335,14 +372,20 @@ __global__ void __launch_bounds__(128) adams_persistent_kernel(const AdamsArgs a
     } else {
       int64_t calls = 0;
       for (;;) {
-        if (calls >= a.max_attempts) {
-          status = kStMaxAttempts;
-          break;
-        }
-        ++calls;
         double it, iy[D];
         int32_t fail = 0;
-        const int r = ad_step<O, Rhs>(s, p, dyn, it, iy, fail);
+        int r;
+        if (s.rk_left > 0) {
+          r = ad_continue<O, Rhs>(s, p, it, iy);  // the call in progress
+        } else {
+          if (calls >= a.max_attempts) {
+            status = kStMaxAttempts;
+            break;
+          }
+          ++calls;
+          r = ad_step<O, Rhs>(s, p, dyn, it, iy, fail);
+        }
+        if (r == kAdPending) continue;
         if (r == kAdDone) break;
         if (r == kAdFail) {
           status = fail;

@@ -121,11 +121,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_ff_kernel(const
             constexpr float mf = static_cast<float>(m);
             if constexpr (static_cast<double>(mf) == m) {
 #pragma unroll
-              for (int d = 0; d < D; ++d) s[d] = ff_add(s[d], ff_mul_f(K[j][d], mf));
+              for (int d = 0; d < D; ++d) s[d] = ff_mad_f(s[d], K[j][d], mf);
             } else {
               constexpr ff mc = ff_const(m);
 #pragma unroll
-              for (int d = 0; d < D; ++d) s[d] = ff_add(s[d], ff_mul(K[j][d], mc));
+              for (int d = 0; d < D; ++d) s[d] = ff_mad(s[d], K[j][d], mc);
             }
           }
         });
@@ -144,12 +144,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_ff_kernel(const
         if constexpr (e != 0.0) {
           constexpr ff ec = ff_const(e);
 #pragma unroll
-          for (int d = 0; d < D; ++d) ev[d] = ff_add(ev[d], ff_mul(K[j][d], ec));
+          for (int d = 0; d < D; ++d) ev[d] = ff_mad(ev[d], K[j][d], ec);
         }
       });
       ff n2f = ff_mul(ev[0], ev[0]);
 #pragma unroll
-      for (int d = 1; d < D; ++d) n2f = ff_add(n2f, ff_mul(ev[d], ev[d]));
+      for (int d = 1; d < D; ++d) n2f = ff_mad(n2f, ev[d], ev[d]);
       const double n2 = ff_to_double(n2f);
       const double tdt = __dmul_rn(tol, dt);
       const double thr = __dmul_rn(tdt, tdt);
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_ff_kernel(const
           if constexpr (bj != 0.0) {
             constexpr ff bc = ff_const(bj);
 #pragma unroll
-            for (int d = 0; d < D; ++d) yn[d] = ff_add(yn[d], ff_mul(K[j][d], bc));
+            for (int d = 0; d < D; ++d) yn[d] = ff_mad(yn[d], K[j][d], bc);
           }
         });
       }
