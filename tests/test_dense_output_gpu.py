@@ -122,3 +122,39 @@ def test_full_slab_ends_with_capacity_status(engine, oracle):
         else:
             assert sol.status[i] == 0 and sol.accepted[i] == p.accepted
     assert full > 0
+
+
+def test_dense_output_of_failing_systems(engine, oracle):
+    """A system that fails keeps the items it yielded before the failure:
+    the attempt cap (NaN state, no item), MinimumTimeDeltaExceeded (stiff),
+    end <= start (no item); the rest are complete."""
+    b = W.van_der_pol(n=48, seed=61)
+    b.y0 = b.y0.copy()
+    b.y0[0, 3] = np.nan
+    b.params = b.params.copy()
+    b.params[0, 7] = 1e6
+    b.t_end = b.t_end.copy()
+    b.t_end[11] = -1.0
+    sol = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=2, max_attempts=3000, dense=True)
+    assert sol.status[3] == 13 and sol.status[7] == 8 and sol.status[11] == 5
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, max_attempts=3000)
+    paths = [oracle.rk_solve_one(cfg, b.rhs, b.y0[:, i], 0.0, float(b.t_end[i]), params=b.params[:, i],
+                                 traj_cap=4096) for i in range(b.n)]
+    np.testing.assert_array_equal(sol.status, [p.status for p in paths])
+    _check_packed(sol, paths, 2)
+
+
+def test_dense_fp32_stage_matches_its_slab(engine):
+    """The FP32-stage kernel writes the same items packed as into slabs."""
+    b = W.lorenz(n=1 << 20).subset(np.arange(0, 1 << 20, 8192))
+    b.t_end = np.minimum(b.t_end, 3.0)
+    kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2, precision=2)
+    slab = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, traj_cap=4096, **kw)
+    dense = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, dense=True, **kw)
+    assert (slab.status == 0).all()
+    off = dense.traj_off
+    for i in range(b.n):
+        k = int(slab.accepted[i])
+        np.testing.assert_array_equal(dense.traj_t[off[i]:off[i + 1]], slab.traj_t[i, :k])
+        np.testing.assert_array_equal(dense.traj_y[off[i]:off[i + 1]], slab.traj_y[i, :k])

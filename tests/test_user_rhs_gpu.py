@@ -26,9 +26,13 @@ SRC = os.path.join(ROOT, "tests", "user_rhs", "user_rhs.cu")
 
 
 @pytest.fixture(scope="module")
-def user_lib(tmp_path_factory):
+def user_lib():
+    """The caller's library, built in-tree (tests/user_rhs/_build, not
+    tracked) as a user's build would place it."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    out = str(tmp_path_factory.mktemp("user_rhs") / "libuser_rhs.so")
+    bdir = os.path.join(ROOT, "tests", "user_rhs", "_build")
+    os.makedirs(bdir, exist_ok=True)
+    out = os.path.join(bdir, "libuser_rhs.so")
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O3",
                     "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
                     "-I", os.path.join(ROOT, "bacon_gb300", "csrc"), SRC, "-o", out], check=True)
