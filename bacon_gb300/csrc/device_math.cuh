@@ -163,13 +163,14 @@ __device__ __forceinline__ double rootn_fix(double z, double r, double adj) {
 // (tol / (2 err)).powf(N.recip()) (src/ivp/adams.rs:527-528, :551-552).  The
 // rounded exponent is 1/N + delta (delta = +2^-54/5, -2^-54/3), so the value
 // is the true root times 1 + delta ln x.  Exponent split x = 2^(Nq) z with z
-// in [1, 2^N), a log-linear first guess from the bit pattern, five Newton
-// steps and an ulp-step correction give the true root; ln x (exponent plus a
+// in [1, 2^N), an FP32 first guess, two Newton steps and an ulp-step
+// correction give the true root; ln x (exponent plus a
 // short atanh series, relative error < 1e-5) moves it by the factor
 // 1 + delta ln x, and a second ulp-step correction on the residual of the
-// radicand z (1 + N delta ln x) rounds it.  The same operation sequence as
-// the CPU oracle's oracle_rootn; correctly rounded except within ~2^-50 ulp
-// of a midpoint.  0 -> 0, inf -> inf, negative or NaN -> NaN (as pow).
+// radicand z (1 + N delta ln x) rounds it.  From the first correction on, the
+// same operation sequence as the CPU oracle's oracle_rootn; correctly rounded
+// except within ~2^-50 ulp of a midpoint.  0 -> 0, inf -> inf, negative or
+// NaN -> NaN (as pow).
 template <int N>
 __device__ __forceinline__ double rootn(double x) {
   static_assert(N == 3 || N == 5, "orders 3 and 5");
@@ -191,16 +192,25 @@ __device__ __forceinline__ double rootn(double x) {
   }
   const double z = __longlong_as_double(
       static_cast<long long>((b & 0x000fffffffffffffull) | (static_cast<unsigned long long>(1023 + rem) << 52)));
-  double y = __longlong_as_double(static_cast<long long>(
-      0x3ff0000000000000ull +
-      (static_cast<unsigned long long>(__double_as_longlong(z)) - 0x3ff0000000000000ull) / N));
+  // The true root z^(1/N) to within one ulp, then the ulp-step correction.
+  // First guess from the FP32 special-function units (log2, exp2: relative
+  // error ~2^-21), then two Newton steps in FP64 whose divisor is an FP32
+  // reciprocal: the error goes 2^-21 -> ~2^-41 -> the rounding of the last
+  // step plus ~0.15 ulp from the rounded y^N, so y is the correctly rounded
+  // root or a neighbour, which is all rootn_fix needs.  (The CPU oracle
+  // starts from a bit-pattern guess with five divided Newton steps; the two
+  // agree after rootn_fix except within ~2^-50 ulp of a rounding midpoint.)
+  // The dependent chain is a third of five divided steps, which matters
+  // because a warp pays for the root whenever any of its lanes needs one.
+  double y = static_cast<double>(exp2f(__fmul_rn(log2f(__double2float_rn(z)), 1.0f / static_cast<float>(N))));
 #pragma unroll
-  for (int it = 0; it < 5; ++it) {
+  for (int it = 0; it < 2; ++it) {
     double ym1 = y;
 #pragma unroll
     for (int k = 2; k < N; ++k) ym1 = __dmul_rn(ym1, y);
     const double yn = __dmul_rn(ym1, y);
-    y = __dsub_rn(y, __ddiv_rn(__dsub_rn(yn, z), __dmul_rn(static_cast<double>(N), ym1)));
+    const float rcp = __frcp_rn(__double2float_rn(__dmul_rn(static_cast<double>(N), ym1)));
+    y = __dsub_rn(y, __dmul_rn(__dsub_rn(yn, z), static_cast<double>(rcp)));
   }
   y = rootn_fix<N>(z, y, 0.0);
   const double m = __longlong_as_double(

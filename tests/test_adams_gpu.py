@@ -123,3 +123,23 @@ def test_euler_builder_dt_averaging(engine):
     path = it.collect_vec()
     ts = np.array([t for t, _ in path])
     np.testing.assert_allclose(np.diff(ts[:5]), 0.015)
+
+
+def test_adams5_vdp_config_full_4096(engine, oracle):
+    """The benchmark's Adams5 workload in full: 4,096 Van der Pol systems to
+    t = 10, ~2.8e9 step calls and ~3e8 fifth roots.  The oracle runs
+    each system on its own host thread pool."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    b = W.van_der_pol()
+    cfg = oracle.adams_cfg(order=5, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+
+    def one(i):
+        return oracle.adams_solve_one(cfg, b.rhs, b.y0[:, i], 0.0, 10.0, params=b.params[:, i])
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        paths = list(ex.map(one, range(b.n)))
+    ref = {"y": np.stack([p.y for p in paths], axis=1), "t": np.array([p.t for p in paths]),
+           "accepted": np.array([p.accepted for p in paths]), "rejected": np.array([p.rejected for p in paths]),
+           "status": np.array([p.status for p in paths], np.int32)}
+    _same(_gpu_adams(engine, b, 5), ref)
