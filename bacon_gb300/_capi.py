@@ -105,6 +105,8 @@ class AdamsOptions(ctypes.Structure):
         ("max_attempts", ctypes.c_int64),
         ("block", ctypes.c_int32),
         ("blocks_per_sm", ctypes.c_int32),
+        ("systems_per_warp", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

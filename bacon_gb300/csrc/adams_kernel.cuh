@@ -39,6 +39,7 @@ struct AdamsArgs {
   int32_t traj_cap;
   int32_t dyn_dim;
   const int64_t* traj_off;  // [n+1] packed offsets, or null: slabs of traj_cap
+  int32_t lanes;            // systems per warp: lanes 0..lanes-1 of each warp take systems
   unsigned long long* queue;
   unsigned long long* first_fail;
 };
@@ -348,6 +349,7 @@ __global__ void __launch_bounds__(128) adams_persistent_kernel(const AdamsArgs a
   constexpr int D = Rhs::DIM;
   constexpr int P = Rhs::NP > 0 ? Rhs::NP : 1;
   const int64_t n = a.n;
+  if (static_cast<int>(threadIdx.x & 31u) >= a.lanes) return;  // idle lane (no block-wide sync below)
   const bool dyn = a.dyn_dim != 0;
   int64_t idx;
   while (next_system(a.queue, n, idx)) {
@@ -428,6 +430,7 @@ __global__ void __launch_bounds__(128) euler_persistent_kernel(const AdamsArgs a
   constexpr int D = Rhs::DIM;
   constexpr int P = Rhs::NP > 0 ? Rhs::NP : 1;
   const int64_t n = a.n;
+  if (static_cast<int>(threadIdx.x & 31u) >= a.lanes) return;  // idle lane (no block-wide sync below)
   int64_t idx;
   while (next_system(a.queue, n, idx)) {
     double p[P], y[D], f[D], last_y[D];

@@ -1104,11 +1104,22 @@ int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double eul
   // One thread runs each system's steps in order, so a batch smaller than
   // the GPU's thread slots is latency bound: each dependent FP64 operation
   // costs ~64 cycles, and warps that share an SM also share its FP64 pipe.
-  // Such a batch is spread thin, down to one warp per SM, instead of filling
-  // a few SMs with 128-thread CTAs.
-  int block = opt->block > 0 ? opt->block : 128;
-  if (opt->block <= 0 && opt->blocks_per_sm <= 0) {
-    const int64_t per_sm = (p->n + c->num_sms - 1) / c->num_sms;
+  // The lanes of a warp are in different phases of the reference's step, so
+  // a warp iteration costs the union of their paths: a small batch runs
+  // fewer systems per warp (more warps, shorter unions), down to ~4 warps per
+  // SM, which is where four latency-bound warps fill one SM's FP64 pipe.
+  int lanes = opt->systems_per_warp;
+  if (lanes < 0 || lanes > 32) return fail(BACON_INVALID_ARGUMENT, "systems_per_warp must be 0..32");
+  if (lanes == 0) {
+    const int64_t per_warp = p->n / (static_cast<int64_t>(c->num_sms) * 4);
+    lanes = 32;
+    while (lanes > 1 && lanes / 2 >= per_warp) lanes /= 2;
+  }
+  a.lanes = lanes;
+  int block = opt->block > 0 ? opt->block : (lanes < 32 ? 32 : 128);
+  if (opt->block <= 0 && opt->blocks_per_sm <= 0 && lanes == 32) {
+    const int64_t warps = (p->n + lanes - 1) / lanes;
+    const int64_t per_sm = (warps + c->num_sms - 1) / c->num_sms * 32;
     if (per_sm < 128) block = static_cast<int>(per_sm <= 32 ? 32 : (per_sm + 31) / 32 * 32);
   }
   if (block % 32 != 0 || block > 128) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 128");
@@ -1121,7 +1132,8 @@ int adams_like_solve(bacon_ctx* c, const bacon_problem* p, int order, double eul
   int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(c->num_sms) * bps;
-  const long long need = (p->n + block - 1) / block;
+  const long long warps_needed = (p->n + lanes - 1) / lanes;
+  const long long need = (warps_needed * 32 + block - 1) / block;
   if (grid > need) grid = need;
   if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
   BACON_CUDA(cudaMemsetAsync(c->d_ctl, 0, sizeof(unsigned long long), c->stream));

@@ -493,13 +493,13 @@ def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_s
 
 def adams_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order=5, max_attempts=0, traj_cap=0,
                 ctx: Context | None = None, block=0, blocks_per_sm=0, dyn_dim=False, out=None,
-                raise_on_error=False, dense=False, dense_capacity=None) -> Solution:
+                raise_on_error=False, dense=False, dense_capacity=None, systems_per_warp=0) -> Solution:
     """Batched Adams5 / Adams3 predictor-corrector (src/ivp/adams.rs); ``dense``
     as rk_solve (bacon_adams_solve_dense)."""
     return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=tol, dt_min=dt_min, dt_max=dt_max, order=order,
                        euler_dt=None, max_attempts=max_attempts, traj_cap=traj_cap, ctx=ctx, block=block,
                        blocks_per_sm=blocks_per_sm, dyn_dim=dyn_dim, out=out, raise_on_error=raise_on_error,
-                       dense=dense, dense_capacity=dense_capacity)
+                       dense=dense, dense_capacity=dense_capacity, systems_per_warp=systems_per_warp)
 
 
 def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx: Context | None = None,
@@ -508,11 +508,11 @@ def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx:
     return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=1.0, dt_min=dt, dt_max=dt, order=1, euler_dt=dt,
                        max_attempts=max_steps, traj_cap=traj_cap, ctx=ctx, block=block,
                        blocks_per_sm=blocks_per_sm, dyn_dim=False, out=out, raise_on_error=raise_on_error,
-                       dense=False, dense_capacity=None)
+                       dense=False, dense_capacity=None, systems_per_warp=0)
 
 
 def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler_dt, max_attempts, traj_cap, ctx,
-                block, blocks_per_sm, dyn_dim, out, raise_on_error, dense, dense_capacity) -> Solution:
+                block, blocks_per_sm, dyn_dim, out, raise_on_error, dense, dense_capacity, systems_per_warp) -> Solution:
     ctx = ctx or default_context()
     device = _is_device(y0)
     if not device:
@@ -529,6 +529,7 @@ def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler
     o.order = 5 if order == 1 else int(order)
     o.memory = MEM_DEVICE if device else MEM_HOST
     o.max_attempts, o.block, o.blocks_per_sm = int(max_attempts), int(block), int(blocks_per_sm)
+    o.systems_per_warp = int(systems_per_warp)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
     L = _capi.load()

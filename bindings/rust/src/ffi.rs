@@ -86,6 +86,8 @@ pub struct bacon_adams_options {
     pub max_attempts: i64,
     pub block: i32,
     pub blocks_per_sm: i32,
+    pub systems_per_warp: i32,
+    pub reserved: i32,
 }
 
 #[repr(C)]

@@ -342,6 +342,14 @@ typedef struct {
   int64_t max_attempts;   /* cap on step() calls per system, 0 = 10,000,000 */
   int32_t block;          /* 0 = 128 */
   int32_t blocks_per_sm;  /* 0 = occupancy model */
+  /* Systems per warp, 1..32 (0 = model).  Each lane runs its system's
+   * steps in order and the lanes of a warp are in different phases of the
+   * reference's step, so a warp iteration costs the union of its lanes'
+   * paths.  Fewer systems per warp shorten that union; more fill the FP64
+   * pipe.  The model takes 32 when the batch fills the GPU and fewer for
+   * small batches. */
+  int32_t systems_per_warp;
+  int32_t reserved;
 } bacon_adams_options;
 
 /* Batched Adams5 / Adams3 (AdamsSolver::step, src/ivp/adams.rs:411-565, with
