@@ -516,6 +516,168 @@ __device__ __forceinline__ void ref_residual(const BdfRefState<O, D>& s, const d
   for (int d = 0; d < D; ++d) out[d] = Op::add(sc[d], y[d]);
 }
 
+// nalgebra's dot product of two vectors of run-time length (blas.rs `dotx`,
+// general path): the rows r0.. of columns cx and cy of a D x D matrix.
+template <int D>
+__device__ __forceinline__ double ref_dotx_col(const double (&x)[D][D], int cx, const double (&y)[D][D], int cy,
+                                               int r0) {
+  using Op = ExactOps;
+  const int len = D - r0;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int i = 0;
+  while (len - i >= 8) {
+    for (int l = 0; l < 8; ++l) acc[l] = Op::add(acc[l], Op::mul(x[r0 + i + l][cx], y[r0 + i + l][cy]));
+    i += 8;
+  }
+  double res = 0.0;
+  res = Op::add(res, Op::add(acc[0], acc[4]));
+  res = Op::add(res, Op::add(acc[1], acc[5]));
+  res = Op::add(res, Op::add(acc[2], acc[6]));
+  res = Op::add(res, Op::add(acc[3], acc[7]));
+  for (int k = i; k < len; ++k) res = Op::add(res, Op::mul(x[r0 + k][cx], y[r0 + k][cy]));
+  return res;
+}
+
+// Rust's f64::signum: 1 for +0 and positives, -1 for -0 and negatives.
+__device__ __forceinline__ double rs_signum(double x) { return isnan(x) ? x : (signbit(x) ? -1.0 : 1.0); }
+
+// nalgebra FullPivLU::new + try_inverse, secant's first fallback
+// (src/ivp/bdf.rs:433-437): the largest |a| of the remaining block, first in
+// column-major order, brought to the diagonal by a column and a row swap,
+// then a Gauss step; invertible when the last diagonal entry is not zero.
+// A cold path, kept out of line.
+template <int D>
+__device__ __noinline__ bool ref_full_piv_lu_inverse(const double (&A)[D][D], double (&inv)[D][D]) {
+  using Op = ExactOps;
+  double a[D][D];
+  int pi[D], pp[D], qi[D], qp[D], np = 0, nq = 0;
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) a[r][c] = A[r][c];
+  for (int i = 0; i < D; ++i) {
+    int pr = i, pc = i;
+    double best = fabs(a[i][i]);
+    for (int c = i; c < D; ++c)
+      for (int r = i; r < D; ++r)
+        if (fabs(a[r][c]) > best) {
+          best = fabs(a[r][c]);
+          pr = r;
+          pc = c;
+        }
+    const double diag = a[pr][pc];
+    if (diag == 0.0) break;  // the rest of the matrix is zero
+    if (pc != i) {
+      for (int r = 0; r < D; ++r) {
+        const double t = a[r][i];
+        a[r][i] = a[r][pc];
+        a[r][pc] = t;
+      }
+      qi[nq] = i;
+      qp[nq] = pc;
+      ++nq;
+    }
+    if (pr != i) {
+      pi[np] = i;
+      pp[np] = pr;
+      ++np;
+      for (int c = 0; c < D; ++c) {
+        const double t = a[i][c];
+        a[i][c] = a[pr][c];
+        a[pr][c] = t;
+      }
+    }
+    const double inv_diag = Op::div(1.0, diag);
+    for (int r = i + 1; r < D; ++r) a[r][i] = Op::mul(a[r][i], inv_diag);
+    for (int c = i + 1; c < D; ++c) {
+      const double alpha = -a[i][c];
+      for (int r = i + 1; r < D; ++r) a[r][c] = Op::add(Op::mul(alpha, a[r][i]), a[r][c]);
+    }
+  }
+  if (a[D - 1][D - 1] == 0.0) return false;
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) inv[r][c] = (r == c) ? 1.0 : 0.0;
+  for (int k = 0; k < np; ++k)
+    for (int c = 0; c < D; ++c) {
+      const double t = inv[pi[k]][c];
+      inv[pi[k]][c] = inv[pp[k]][c];
+      inv[pp[k]][c] = t;
+    }
+  for (int k = 0; k < D; ++k)
+    for (int i = 0; i < D - 1; ++i) {
+      const double mc = -Op::div(inv[i][k], 1.0);
+      for (int r = i + 1; r < D; ++r) inv[r][k] = Op::add(Op::mul(mc, a[r][i]), inv[r][k]);
+    }
+  for (int k = 0; k < D; ++k)
+    for (int i = D - 1; i >= 0; --i) {
+      const double diag = a[i][i];
+      if (diag == 0.0) break;  // try_inverse ignores the solve's own result
+      const double coeff = Op::div(inv[i][k], diag);
+      inv[i][k] = coeff;
+      const double mc = -coeff;
+      for (int r = 0; r < i; ++r) inv[r][k] = Op::add(Op::mul(mc, a[r][i]), inv[r][k]);
+    }
+  for (int k = nq - 1; k >= 0; --k)
+    for (int c = 0; c < D; ++c) {
+      const double t = inv[qi[k]][c];
+      inv[qi[k]][c] = inv[qp[k]][c];
+      inv[qp[k]][c] = t;
+    }
+  return true;
+}
+
+// nalgebra QR::new (Householder reflections: householder.rs
+// clear_column_unchecked, reflection_axis_mut) + try_inverse (Q^T by the
+// stored reflections, then the upper solve on R's diagonal), secant's second
+// fallback (src/ivp/bdf.rs:438-440).  False when a diagonal entry of R is 0.
+template <int D>
+__device__ __noinline__ bool ref_qr_inverse(const double (&A)[D][D], double (&inv)[D][D]) {
+  using Op = ExactOps;
+  double a[D][D], diag[D];
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) a[r][c] = A[r][c];
+  for (int i = 0; i < D; ++i) {
+    const double sq = Op::add(0.0, ref_dotx_col(a, i, a, i, i));
+    const double nrm = Op::sqrt(sq);
+    const double x0 = a[i][i];
+    const double modulus = (x0 >= 0.0) ? x0 : -x0;
+    const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+    const double signed_norm = Op::mul(sgn, nrm);
+    const double factor = Op::mul(Op::add(sq, Op::mul(modulus, nrm)), 2.0);
+    a[i][i] = Op::add(a[i][i], signed_norm);
+    if (factor != 0.0) {
+      const double sf = Op::sqrt(factor);
+      for (int r = i; r < D; ++r) a[r][i] = Op::div(a[r][i], sf);
+      diag[i] = -signed_norm;
+      const double sign = rs_signum(diag[i]);
+      const double m_two = Op::mul(sign, -2.0);
+      for (int c = i + 1; c < D; ++c) {
+        const double f = Op::mul(Op::sub(ref_dotx_col(a, i, a, c, i), 0.0), m_two);
+        for (int r = i; r < D; ++r) a[r][c] = Op::add(Op::mul(f, a[r][i]), Op::mul(sign, a[r][c]));
+      }
+    } else {
+      diag[i] = signed_norm;
+    }
+  }
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) inv[r][c] = (r == c) ? 1.0 : 0.0;
+  for (int i = 0; i < D; ++i) {
+    const double sign = rs_signum(diag[i]);
+    const double m_two = Op::mul(sign, -2.0);
+    for (int c = 0; c < D; ++c) {
+      const double f = Op::mul(Op::sub(ref_dotx_col(a, i, inv, c, i), 0.0), m_two);
+      for (int r = i; r < D; ++r) inv[r][c] = Op::add(Op::mul(f, a[r][i]), Op::mul(sign, inv[r][c]));
+    }
+  }
+  for (int k = 0; k < D; ++k)
+    for (int i = D - 1; i >= 0; --i) {
+      if (diag[i] == 0.0) return false;
+      const double coeff = Op::div(inv[i][k], diag[i]);
+      inv[i][k] = coeff;
+      const double mc = -coeff;
+      for (int r = 0; r < i; ++r) inv[r][k] = Op::add(Op::mul(mc, a[r][i]), inv[r][k]);
+    }
+  return true;
+}
+
 // nalgebra LU::new + try_inverse (partial pivoting, first maximum).
 template <int D>
 __device__ bool ref_lu_inverse(const double (&A)[D][D], double (&inv)[D][D]) {
@@ -620,7 +782,10 @@ __device__ int32_t ref_secant(const BdfRefState<O, D>& s, const double* p, bool 
       if (d == c) guess[d] = gc;
     for (int r = 0; r < D; ++r) jac[r][c] = Op::mul(Op::add(above[r], below[r]), denom);
   }
-  if (!ref_lu_inverse(jac, inv)) return kStSingular;
+  // lu().try_inverse(), else full_piv_lu().try_inverse(), else
+  // qr().try_inverse(), else SingularMatrix (src/ivp/bdf.rs:429-443)
+  if (!ref_lu_inverse(jac, inv) && !ref_full_piv_lu_inverse(jac, inv) && !ref_qr_inverse(jac, inv))
+    return kStSingular;
   for (int r = 0; r < D; ++r)
     for (int c = 0; c < D; ++c) minv[r][c] = -inv[r][c];
   ref_gemv(minv, deriv, shift);

@@ -16,9 +16,11 @@
  * t -= dt - order on a rejected bootstrap).  nalgebra 0.32's LU (partial
  * pivoting, first maximum of |a|, multiplication by the reciprocal pivot),
  * its triangular solves and its gemv accumulation order are restated from
- * its published source.  The full-pivot LU and QR fallbacks of secant
- * (bdf.rs:433-443) are only reached for a matrix whose partial-pivot LU has
- * an exactly zero pivot; the restatement reports SingularMatrix there.
+ * its published algorithms, and so are the full-pivot LU and Householder QR
+ * that secant falls back to (bdf.rs:433-443) when the partial-pivot LU has an
+ * exactly zero pivot.  The "+" finite difference makes the Jacobian's columns
+ * nearly equal, so on multi-dimensional systems that happens (Lotka-Volterra,
+ * Lorenz).
  *
  * ORC_BDF_CORRECTED is this engine's stiff BDF (no reference counterpart to
  * follow beyond the structure above): orders 1..6 ramped up after every
@@ -103,6 +105,150 @@ static int lu_try_inverse(const dmat A, int n, dmat inv) {
       for (int r = 0; r < i; ++r) inv[r][k] = (mc * a[r][i]) + inv[r][k];
     }
   }
+  return 1;
+}
+
+/* nalgebra's dot product of two vectors of run-time length (blas.rs `dotx`,
+ * the general path: eight accumulators over whole blocks of eight, folded
+ * pairwise into res, then the remaining products added in order).  x and y
+ * are columns of row-major n x n matrices starting at row r0: element k is
+ * x[(r0 + k) * ORC_MAX_BDF_DIM]. */
+static double dotx_col(const double* x, const double* y, int len) {
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int i = 0;
+  while (len - i >= 8) {
+    for (int l = 0; l < 8; ++l) acc[l] = acc[l] + (x[(i + l) * ORC_MAX_BDF_DIM] * y[(i + l) * ORC_MAX_BDF_DIM]);
+    i += 8;
+  }
+  double res = 0.0;
+  res = res + (acc[0] + acc[4]);
+  res = res + (acc[1] + acc[5]);
+  res = res + (acc[2] + acc[6]);
+  res = res + (acc[3] + acc[7]);
+  for (int k = i; k < len; ++k) res = res + (x[k * ORC_MAX_BDF_DIM] * y[k * ORC_MAX_BDF_DIM]);
+  return res;
+}
+
+/* Rust's f64::signum: 1 for +0 and positives, -1 for -0 and negatives. */
+static double rs_signum(double x) { return isnan(x) ? x : (signbit(x) ? -1.0 : 1.0); }
+
+/* nalgebra FullPivLU::new (the largest |a| of the remaining block, first in
+ * column-major order, swapped into place by a column and a row swap, then a
+ * Gauss step), then try_inverse: row permutation, unit-lower and upper
+ * solves, inverse column permutation.  Returns 0 when the last diagonal
+ * entry is exactly zero (is_invertible). */
+static int full_piv_lu_try_inverse(const dmat A, int n, dmat inv) {
+  static __thread dmat a;
+  int pi[ORC_MAX_BDF_DIM], pp[ORC_MAX_BDF_DIM], qi[ORC_MAX_BDF_DIM], qp[ORC_MAX_BDF_DIM], np = 0, nq = 0;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) a[r][c] = A[r][c];
+  for (int i = 0; i < n; ++i) {
+    int pr = i, pc = i;
+    double best = fabs(a[i][i]);
+    for (int c = i; c < n; ++c)
+      for (int r = i; r < n; ++r)
+        if (fabs(a[r][c]) > best) {
+          best = fabs(a[r][c]);
+          pr = r;
+          pc = c;
+        }
+    const double diag = a[pr][pc];
+    if (diag == 0.0) break; /* the rest of the matrix is zero */
+    if (pc != i) {
+      for (int r = 0; r < n; ++r) { const double t = a[r][i]; a[r][i] = a[r][pc]; a[r][pc] = t; }
+      qi[nq] = i;
+      qp[nq] = pc;
+      ++nq;
+    }
+    if (pr != i) {
+      pi[np] = i;
+      pp[np] = pr;
+      ++np;
+      for (int c = 0; c < n; ++c) { const double t = a[i][c]; a[i][c] = a[pr][c]; a[pr][c] = t; }
+    }
+    const double inv_diag = 1.0 / diag;
+    for (int r = i + 1; r < n; ++r) a[r][i] = a[r][i] * inv_diag;
+    for (int c = i + 1; c < n; ++c) {
+      const double alpha = -a[i][c];
+      for (int r = i + 1; r < n; ++r) a[r][c] = (alpha * a[r][i]) + a[r][c];
+    }
+  }
+  if (a[n - 1][n - 1] == 0.0) return 0;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) inv[r][c] = (r == c) ? 1.0 : 0.0;
+  for (int k = 0; k < np; ++k)
+    for (int c = 0; c < n; ++c) { const double t = inv[pi[k]][c]; inv[pi[k]][c] = inv[pp[k]][c]; inv[pp[k]][c] = t; }
+  for (int k = 0; k < n; ++k)
+    for (int i = 0; i < n - 1; ++i) {
+      const double mc = -(inv[i][k] / 1.0);
+      for (int r = i + 1; r < n; ++r) inv[r][k] = (mc * a[r][i]) + inv[r][k];
+    }
+  for (int k = 0; k < n; ++k)
+    for (int i = n - 1; i >= 0; --i) {
+      const double diag = a[i][i];
+      if (diag == 0.0) break; /* the solve's own result is ignored by try_inverse */
+      const double coeff = inv[i][k] / diag;
+      inv[i][k] = coeff;
+      const double mc = -coeff;
+      for (int r = 0; r < i; ++r) inv[r][k] = (mc * a[r][i]) + inv[r][k];
+    }
+  for (int k = nq - 1; k >= 0; --k)
+    for (int c = 0; c < n; ++c) { const double t = inv[qi[k]][c]; inv[qi[k]][c] = inv[qp[k]][c]; inv[qp[k]][c] = t; }
+  return 1;
+}
+
+/* nalgebra QR::new (Householder reflections, householder.rs
+ * clear_column_unchecked / reflection_axis_mut) then try_inverse (Q^T by the
+ * stored reflections, then the upper solve with R's diagonal).  Returns 0
+ * when a diagonal entry of R is exactly zero. */
+static int qr_try_inverse(const dmat A, int n, dmat inv) {
+  static __thread dmat a;
+  double diag[ORC_MAX_BDF_DIM];
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) a[r][c] = A[r][c];
+  for (int i = 0; i < n; ++i) {
+    const int len = n - i;
+    const double sq = 0.0 + dotx_col(&a[i][i], &a[i][i], len);
+    const double nrm = sqrt(sq);
+    const double x0 = a[i][i];
+    const double modulus = (x0 >= 0.0) ? x0 : -x0;
+    const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+    const double signed_norm = sgn * nrm;
+    const double factor = (sq + (modulus * nrm)) * 2.0;
+    a[i][i] = a[i][i] + signed_norm;
+    if (factor != 0.0) {
+      const double sf = sqrt(factor);
+      for (int r = i; r < n; ++r) a[r][i] = a[r][i] / sf;
+      diag[i] = -signed_norm;
+      const double sign = rs_signum(diag[i]);
+      const double m_two = sign * -2.0;
+      for (int c = i + 1; c < n; ++c) {
+        const double f = (dotx_col(&a[i][i], &a[i][c], len) - 0.0) * m_two;
+        for (int r = i; r < n; ++r) a[r][c] = (f * a[r][i]) + (sign * a[r][c]);
+      }
+    } else {
+      diag[i] = signed_norm;
+    }
+  }
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) inv[r][c] = (r == c) ? 1.0 : 0.0;
+  for (int i = 0; i < n; ++i) {
+    const int len = n - i;
+    const double sign = rs_signum(diag[i]);
+    const double m_two = sign * -2.0;
+    for (int c = 0; c < n; ++c) {
+      const double f = (dotx_col(&a[i][i], &inv[i][c], len) - 0.0) * m_two;
+      for (int r = i; r < n; ++r) inv[r][c] = (f * a[r][i]) + (sign * inv[r][c]);
+    }
+  }
+  for (int k = 0; k < n; ++k)
+    for (int i = n - 1; i >= 0; --i) {
+      if (diag[i] == 0.0) return 0;
+      const double coeff = inv[i][k] / diag[i];
+      inv[i][k] = coeff;
+      const double mc = -coeff;
+      for (int r = 0; r < i; ++r) inv[r][k] = (mc * a[r][i]) + inv[r][k];
+    }
   return 1;
 }
 
@@ -198,7 +344,10 @@ static int32_t ref_secant(bdf_ref* s, int lower, double* result) {
     guess[c] = guess[c] + s->dt;
     for (int r = 0; r < n; ++r) jac[r][c] = (above[r] + below[r]) * denom;
   }
-  if (!lu_try_inverse(jac, n, inv)) return ORC_SINGULAR_MATRIX;
+  /* lu().try_inverse(), else full_piv_lu().try_inverse(), else
+   * qr().try_inverse(), else SingularMatrix (bdf.rs:429-443) */
+  if (!lu_try_inverse(jac, n, inv) && !full_piv_lu_try_inverse(jac, n, inv) && !qr_try_inverse(jac, n, inv))
+    return ORC_SINGULAR_MATRIX;
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c) minv[r][c] = -inv[r][c];
   gemv_cols(minv, deriv, n, shift);
@@ -700,3 +849,22 @@ int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, doubl
   corrected_solve(n, M, piv, rinv, x);
   return 1;
 }
+
+/* The inverse secant takes (a test hook): A row-major n x n.  Returns 1 for
+ * the partial-pivot LU, 2 for the full-pivot LU fallback, 3 for the QR
+ * fallback, 0 when all three fail (SingularMatrix). */
+int oracle_bdf_secant_inverse(int32_t n, const double* A, double* inv) {
+  static __thread dmat M, R;
+  if (n < 1 || n > ORC_MAX_BDF_DIM) return -1;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) M[r][c] = A[r * n + c];
+  int which = 0;
+  if (lu_try_inverse(M, n, R)) which = 1;
+  else if (full_piv_lu_try_inverse(M, n, R)) which = 2;
+  else if (qr_try_inverse(M, n, R)) which = 3;
+  if (which)
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) inv[r * n + c] = R[r][c];
+  return which;
+}
+

@@ -158,6 +158,10 @@ int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, doubl
  * least (one per distinct h*b_q of a solve for the constant-Jacobian chains,
  * one per Newton solve otherwise)}.  reset != 0 zeroes the counters. */
 void oracle_bdf_work(int64_t* out3, int reset);
+/* The inverse the as-compiled BDF's secant takes for a row-major n x n
+ * matrix A: 1 partial-pivot LU, 2 full-pivot LU, 3 QR (src/ivp/bdf.rs:429-443),
+ * 0 when all fail (SingularMatrix).  Test hook. */
+int oracle_bdf_secant_inverse(int32_t n, const double* A, double* inv);
 
 /* ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) -- */
 typedef struct {

@@ -110,6 +110,8 @@ def lib():
             L.oracle_corrected_linsolve.argtypes = [ctypes.c_int32, dp, dp, dp]
             L.oracle_bdf_work.restype = None
             L.oracle_bdf_work.argtypes = [lp, ctypes.c_int]
+            L.oracle_bdf_secant_inverse.restype = ctypes.c_int
+            L.oracle_bdf_secant_inverse.argtypes = [ctypes.c_int32, dp, dp]
         if hasattr(L, "oracle_adams_solve_one"):
             L.oracle_rootn.restype = ctypes.c_double
             L.oracle_rootn.argtypes = [ctypes.c_double, ctypes.c_int]
@@ -305,6 +307,15 @@ def bdf_solve_one(cfg, rhs, y0, t0, t_end, params=None, shared=None, traj_cap=0)
         n = min(a.value, traj_cap)
         tt, ty = tt[:n], ty[:n]
     return Path(st, t.value, y, a.value, r.value, tt, ty)
+
+
+def bdf_secant_inverse(A):
+    """(which, inverse) of the as-compiled BDF's secant: 1 partial-pivot LU,
+    2 full-pivot LU, 3 QR, 0 SingularMatrix (inverse None)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    inv = np.zeros_like(A)
+    which = lib().oracle_bdf_secant_inverse(A.shape[0], _dp(A), _dp(inv))
+    return which, (inv if which > 0 else None)
 
 
 def bdf_work(reset: bool = True) -> dict:

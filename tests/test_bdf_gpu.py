@@ -119,3 +119,21 @@ def test_corrected_reference_tests_via_builder(engine):
         assert len(path) > 0
         for t, y in path:
             assert abs(y[0] - exact(t)) <= eps
+
+
+@pytest.mark.parametrize("kind", ["lorenz", "lotka_volterra"])
+def test_as_compiled_secant_fallbacks(engine, oracle, kind):
+    """The reference's secant on multi-dimensional systems: the "+" finite
+    difference makes the Jacobian's columns nearly equal, its partial-pivot
+    LU meets exactly zero pivots, and the full-pivot LU and QR fallbacks
+    (src/ivp/bdf.rs:433-443) take over.  Bit for bit against the oracle,
+    including the systems where all three fail (SingularMatrix)."""
+    if kind == "lorenz":
+        b = W.lorenz(n=64, seed=5)
+        b.t_end = np.full(b.n, 2.0)
+    else:
+        b = W.lotka_volterra(n=64, seed=6)
+        b.t_end = np.full(b.n, 5.0)
+    sol = _gpu(engine, b, engine.BDF_AS_COMPILED, max_steps=20000)
+    ref = _oracle(oracle, b, oracle.BDF_AS_COMPILED, max_steps=20000)
+    _same(sol, ref)

@@ -80,3 +80,27 @@ def test_zero_pivot_reported(oracle):
     A = np.zeros((5, 5))
     A[0, 0] = 1.0
     assert oracle.corrected_linsolve(A, np.ones(5)) is None
+
+
+def test_secant_fallbacks_full_pivot_lu_and_qr(oracle):
+    """secant inverts its finite-difference Jacobian with nalgebra's LU, then
+    full-pivot LU, then QR, then fails with SingularMatrix
+    (src/ivp/bdf.rs:429-443).  The "+" finite difference makes the columns
+    nearly equal, so the fallbacks are reached on multi-dimensional systems.
+    Matrices with one row a multiple of another (exactly singular before
+    rounding) take each path: the rounding of the elimination decides which
+    factorisation ends with an exactly zero pivot."""
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(4, 4))
+    which, inv = oracle.bdf_secant_inverse(A)
+    assert which == 1
+    np.testing.assert_allclose(A @ inv, np.eye(4), atol=1e-12)
+    r0 = np.array([3 / 7, 0.2, 1 / 3])
+    full = np.stack([r0, np.array([1.5, -0.6, -1.0]), r0 * 0.3])
+    which, inv = oracle.bdf_secant_inverse(full)
+    assert which == 2 and np.all(np.isfinite(inv))
+    q0 = np.array([5.0, 3 / 7])
+    which, inv = oracle.bdf_secant_inverse(np.stack([q0, q0 * 0.5]))
+    assert which == 3 and np.all(np.isfinite(inv))
+    which, inv = oracle.bdf_secant_inverse(np.array([[0.0, 1.0], [0.0, 1.0]]))
+    assert which == 0 and inv is None
