@@ -751,8 +751,8 @@ pub fn solve_mixed(ctx: &mut Context, uniform: Option<&GpuBdf6>, ragged: Option<
             uprob.as_ref().map_or(ptr::null(), |p| p as *const _),
             rprob.as_ref().map_or(ptr::null(), |p| p as *const _),
             &opts,
-            if uniform.is_some() { &mut ures } else { ptr::null_mut() },
-            if ragged.is_some() { &mut rres } else { ptr::null_mut() },
+            if uniform.is_some() { &mut ures as *mut ffi::bacon_rk_result } else { ptr::null_mut() },
+            if ragged.is_some() { &mut rres as *mut ffi::bacon_ragged_result } else { ptr::null_mut() },
         )
     };
     batch_ok(code)?;
