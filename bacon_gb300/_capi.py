@@ -213,6 +213,9 @@ SIGNATURES = {
                                             ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
     "bacon_bdf_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(BdfOptions),
                                              ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
+    "bacon_euler_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.c_double,
+                                               ctypes.POINTER(AdamsOptions), ctypes.POINTER(RkResult),
+                                               ctypes.POINTER(DenseOutput)]),
     "bacon_adams_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(AdamsOptions),
                                                ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
     "bacon_rk_solve_noalloc": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),

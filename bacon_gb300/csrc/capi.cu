@@ -1564,6 +1564,14 @@ extern "C" int bacon_adams_solve_dense(bacon_ctx* c, const bacon_problem* p, con
   return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_adams_solve(c, p, opt, r); });
 }
 
+extern "C" int bacon_euler_solve_dense(bacon_ctx* c, const bacon_problem* p, double dt,
+                                       const bacon_adams_options* opt, bacon_rk_result* r,
+                                       bacon_dense_output* dense) {
+  NvtxRange nvtx_range("bacon_euler_solve_dense");
+  if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
+  return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_euler_solve(c, p, dt, opt, r); });
+}
+
 // ---------------------------------------------------------------------------
 // Autotuner: times the persistent kernel on the caller's own batch for a set
 // of launch shapes and caches the fastest for this kernel and batch size.

@@ -503,12 +503,14 @@ def adams_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order=5, max
 
 
 def euler_solve(y0, params, t0, t_end, *, rhs, dt, max_steps=0, traj_cap=0, ctx: Context | None = None,
-                block=0, blocks_per_sm=0, out=None, raise_on_error=False) -> Solution:
-    """Batched Euler with a fixed step dt (src/ivp.rs:240-485)."""
+                block=0, blocks_per_sm=0, out=None, raise_on_error=False, dense=False,
+                dense_capacity=None) -> Solution:
+    """Batched Euler with a fixed step dt (src/ivp.rs:240-485); ``dense`` as
+    rk_solve (bacon_euler_solve_dense)."""
     return _adams_like(y0, params, t0, t_end, rhs=rhs, tol=1.0, dt_min=dt, dt_max=dt, order=1, euler_dt=dt,
                        max_attempts=max_steps, traj_cap=traj_cap, ctx=ctx, block=block,
                        blocks_per_sm=blocks_per_sm, dyn_dim=False, out=out, raise_on_error=raise_on_error,
-                       dense=False, dense_capacity=None, systems_per_warp=0)
+                       dense=dense, dense_capacity=dense_capacity, systems_per_warp=0)
 
 
 def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler_dt, max_attempts, traj_cap, ctx,
@@ -534,8 +536,12 @@ def _adams_like(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order, euler
         out = alloc_outputs(dim, n, device, traj_cap)
     L = _capi.load()
     if dense:
-        code, tt, ty, off = _dense_call(L.bacon_adams_solve_dense, ctx.handle, prob, o, out, device, dim, n,
-                                        dense_capacity)
+        if euler_dt is None:
+            fn = L.bacon_adams_solve_dense
+        else:
+            def fn(h, pr, op, rs, dz):
+                return L.bacon_euler_solve_dense(h, pr, float(euler_dt), op, rs, dz)
+        code, tt, ty, off = _dense_call(fn, ctx.handle, prob, o, out, device, dim, n, dense_capacity)
         if code in (14, 15, 16) or (raise_on_error and code != 0):
             raise IVPError(code, _capi.last_error())
         return Solution(out["y"], out["t"], out["accepted"], out["rejected"], out["status"], int(code), tt, ty, off)

@@ -285,6 +285,14 @@ extern "C" {
         result: *mut bacon_rk_result,
         dense: *mut bacon_dense_output,
     ) -> c_int;
+    pub fn bacon_euler_solve_dense(
+        ctx: *mut bacon_ctx,
+        problem: *const bacon_problem,
+        dt: f64,
+        options: *const bacon_adams_options,
+        result: *mut bacon_rk_result,
+        dense: *mut bacon_dense_output,
+    ) -> c_int;
     pub fn bacon_adams_solve_dense(
         ctx: *mut bacon_ctx,
         problem: *const bacon_problem,

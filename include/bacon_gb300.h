@@ -433,7 +433,8 @@ typedef struct {
   int64_t total;     /* out: items of the whole batch, offsets[n] */
 } bacon_dense_output;
 
-/* bacon_rk_solve / bacon_bdf_solve / bacon_adams_solve with dense output.
+/* bacon_rk_solve / bacon_bdf_solve / bacon_adams_solve / bacon_euler_solve
+ * with dense output.
  * Two passes: the first solve counts each system's items, an exclusive scan
  * of the counts gives the offsets, and a second solve (bit-identical to the
  * first) writes each item to its slot.  If total > capacity the call returns
@@ -449,6 +450,9 @@ int bacon_bdf_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const ba
                           bacon_rk_result* result, bacon_dense_output* dense);
 int bacon_adams_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_adams_options* options,
                             bacon_rk_result* result, bacon_dense_output* dense);
+int bacon_euler_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, double dt,
+                            const bacon_adams_options* options, bacon_rk_result* result,
+                            bacon_dense_output* dense);
 
 /* ---- discrete adjoint ---------------------------------------------------- */
 /* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with

@@ -158,3 +158,13 @@ def test_dense_fp32_stage_matches_its_slab(engine):
         k = int(slab.accepted[i])
         np.testing.assert_array_equal(dense.traj_t[off[i]:off[i + 1]], slab.traj_t[i, :k])
         np.testing.assert_array_equal(dense.traj_y[off[i]:off[i + 1]], slab.traj_y[i, :k])
+
+
+def test_euler_dense_matches_oracle_path(engine, oracle):
+    """Euler yields the state each step starts from (src/ivp.rs:318-339)."""
+    b = W.van_der_pol(n=64, seed=67)
+    sol = engine.euler_solve(b.y0, b.params, 0.0, 2.0, rhs=b.rhs, dt=0.01, dense=True)
+    assert sol.code == 0
+    paths = [oracle.euler_solve_one(b.rhs, b.y0[:, i], 0.0, 2.0, 0.01, params=b.params[:, i], traj_cap=4096)
+             for i in range(b.n)]
+    _check_packed(sol, paths, 2)
