@@ -1,6 +1,6 @@
 """Run one benchmark workload once, device-resident, and print a JSON summary.
 
-    python -m bacon_gb300.cases lorenz --n 131072 [--precision fp32_comp]
+    python -m bacon_gb300.cases lorenz --n 131072 [--precision fp32_comp] [--tuned 1,256,4]
     python -m bacon_gb300.cases stiff --n 8192
     python -m bacon_gb300.cases chains --n 4096
     python -m bacon_gb300.cases linear --n 8192 [--precision tc_split]
@@ -12,6 +12,8 @@ Each case generates the workload's seeded batch at the given size (the
 workload generators in workloads.py), solves it `--repeat` times through the
 engine's public calls and prints the last solve's kernel time and status
 counts.  It is the small, self-contained command the profiles cite.
+``--tuned VARIANT,BLOCK,CTAS_PER_SM`` pins the RK kernel variant and launch
+shape (bacon_rk_set_tuned), e.g. the ones the benchmark's autotuner chose.
 """
 from __future__ import annotations
 
@@ -46,7 +48,7 @@ def _counts(status):
     return {int(k): int((s == k).sum()) for k in np.unique(s)}
 
 
-def run(case: str, n: int, precision: str, repeat: int) -> dict:
+def run(case: str, n: int, precision: str, repeat: int, tuned: tuple | None = None) -> dict:
     import torch
     ctx = E.Context(0)
     prec = PRECISION[precision]
@@ -57,6 +59,9 @@ def run(case: str, n: int, precision: str, repeat: int) -> dict:
         if case in ("lorenz", "vdp"):
             b = W.lorenz(n=n) if case == "lorenz" else W.van_der_pol(n=n)
             y0, p, ts, te = _dev(torch, b.y0, b.params, b.t0, b.t_end)
+            if tuned is not None:
+                E.rk_set_tuned(y0, rhs=b.rhs, variant=tuned[0], block=tuned[1], blocks_per_sm=tuned[2],
+                               layout=E.FEHLBERG, precision=prec, ctx=ctx)
             s = E.rk_solve(y0, p, ts, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
                            layout=E.FEHLBERG, precision=prec, ctx=ctx)
             out["status"] = _counts(s.status)
@@ -105,8 +110,12 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--precision", default="fp64_exact", choices=sorted(PRECISION))
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--tuned", default=None, help="VARIANT,BLOCK,CTAS_PER_SM for lorenz / vdp")
     a = ap.parse_args()
-    print(json.dumps(run(a.case, a.n, a.precision, a.repeat)))
+    tuned = tuple(int(x) for x in a.tuned.split(",")) if a.tuned else None
+    if tuned is not None and len(tuned) != 3:
+        raise SystemExit("--tuned wants VARIANT,BLOCK,CTAS_PER_SM")
+    print(json.dumps(run(a.case, a.n, a.precision, a.repeat, tuned)))
 
 
 if __name__ == "__main__":
