@@ -259,6 +259,7 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
       dn = O::add(dn, O::mul(dx[d], dx[d]));
     }
     if (!(dn == dn)) return false;
+    if constexpr (Rhs::kAffine) return true;  // the first update solves the linear system
     if (O::sqrt(dn) <= conv) return true;
   }
   return false;

@@ -211,6 +211,7 @@ struct RaggedArgs {
 // N..2N-1 the forces; y and p in shared memory.  Same expressions as RhsChain
 // and the oracle's chain right-hand side.
 struct RagChain {
+  static constexpr bool kAffine = true;  // f = J y, J constant
   __device__ __forceinline__ static double f(int r, int N, const double* y, const double* p) {
     using O = ExactOps;
     if (r < N) return y[N + r];
@@ -693,6 +694,10 @@ __device__ __forceinline__ bool rag_newton(RagGroup& g, int D, int N, const doub
     // when some dx is NaN.
     const double part = g.sum(own ? O::mul(dx, dx) : 0.0);
     if (!(part == part)) return false;
+    // The chain is affine in y and M holds its exact Jacobian, so the first
+    // update solves the linear system: the solve ends here (the oracle's
+    // rule for affine right-hand sides).
+    if (RagChain::kAffine) return true;
     const double thr = O::mul(conv, conv);
     if (fabs(O::sub(part, thr)) > O::mul(1e-10, thr)) {
       if (part < thr) return true;
@@ -748,14 +753,44 @@ __device__ __forceinline__ double rag_norm_decide(RagGroup& g, int D, const doub
   return rag_norm(g, D, sv);
 }
 
-// Interpolates this thread's k history values onto nodes -s*j (j < k).
-__device__ __forceinline__ void rag_interp_row(int r, int ld, int k, double s, const double* src, double* dst) {
+// Lagrange weights the ragged steps use at fixed points, computed once per
+// CTA by lagrange_weights itself (so the same values): the predictor's, at
+// s = 1 over k = 1..7 history points, and the halving's, at the nodes
+// s = -0.5 j (j < k).  Each is a division chain of ~k dependent FP64 divisions
+// that every step (or rejection) would otherwise repeat.
+struct RagWeights {
+  double pred[7][7];     // [k-1][i]
+  double half[7][7][7];  // [k-1][j][i]
+};
+
+__device__ __forceinline__ void rag_weights_init(RagWeights& wt) {
+  using O = ExactOps;
+  for (int u = static_cast<int>(threadIdx.x); u < 7 + 49; u += static_cast<int>(blockDim.x)) {
+    double w[7];
+    if (u < 7) {
+      lagrange_weights(u, 1.0, w);
+      for (int i = 0; i <= u; ++i) wt.pred[u][i] = w[i];
+    } else {
+      const int q = (u - 7) / 7, j = (u - 7) % 7;
+      if (j > q) continue;
+      lagrange_weights(q, O::mul(-0.5, static_cast<double>(j)), w);
+      for (int i = 0; i <= q; ++i) wt.half[q][j][i] = w[i];
+    }
+  }
+}
+
+// Interpolates this thread's k history values onto nodes -s*j (j < k), with
+// the weights of the table wt ([j][i]) when given.
+__device__ __forceinline__ void rag_interp_row(int r, int ld, int k, double s, const double* src, double* dst,
+                                               const double (*wt)[7]) {
   using O = ExactOps;
   double w[7];
   for (int j = 0; j < k; ++j) {
-    lagrange_weights(k - 1, O::mul(-s, static_cast<double>(j)), w);
+    const double* wj = w;
+    if (wt != nullptr) wj = wt[j];
+    else lagrange_weights(k - 1, O::mul(-s, static_cast<double>(j)), w);
     double acc = 0.0;
-    for (int i = 0; i < k; ++i) acc = O::add(acc, O::mul(w[i], src[i * ld + r]));
+    for (int i = 0; i < k; ++i) acc = O::add(acc, O::mul(wj[i], src[i * ld + r]));
     dst[j * ld + r] = acc;
   }
 }
@@ -763,7 +798,7 @@ __device__ __forceinline__ void rag_interp_row(int r, int ld, int k, double s, c
 // One ragged system integrated by the calling group; ws is its shared-memory
 // slice for dims <= ld, gcache its device-memory factor slots.
 __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t idx, RagGroup& g, double* ws, int ld,
-                                                 double* gcache) {
+                                                 double* gcache, const RagWeights& wt) {
   using O = ExactOps;
   double* sM = ws + RagSmem::M(ld);
   double* srinv = ws + RagSmem::rinv(ld);
@@ -815,12 +850,11 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
     const int q = (k < qmax) ? k : qmax;
     const double* HHp = H;
     if (h != dt && k > 1) {
-      if (own) rag_interp_row(r, ld, k, O::div(h, dt), H, HH);
+      if (own) rag_interp_row(r, ld, k, O::div(h, dt), H, HH, nullptr);
       HHp = HH;
     }
     // predictor: extrapolation through the history points
-    double w[7];
-    lagrange_weights(k - 1, 1.0, w);
+    const double* w = wt.pred[k - 1];
     double yh = 0.0, yl = 0.0;
     if (own)
       for (int i = 0; i < k; ++i) yh = O::add(yh, O::mul(w[i], HHp[i * ld + r]));
@@ -878,7 +912,7 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
     if (k > 1) {
       g.sync();  // every row has finished reading H
       if (own) {
-        rag_interp_row(r, ld, k, 0.5, H, HH);
+        rag_interp_row(r, ld, k, 0.5, H, HH, wt.half[k - 1]);
         for (int i = 0; i < k; ++i) H[i * ld + r] = HH[i * ld + r];
       }
       g.sync();
@@ -907,6 +941,9 @@ template <class Small>
 __global__ void __launch_bounds__(kRagWarps * 32, 1)
     bdf_mixed_kernel(const BdfArgs small, int small_dyn, const RaggedArgs rg) {
   extern __shared__ __align__(16) double rag_smem[];
+  __shared__ RagWeights rag_w;
+  rag_weights_init(rag_w);
+  __syncthreads();
   const int warp = static_cast<int>(threadIdx.x >> 5);
   double* gcache_cta = rg.gcache + static_cast<size_t>(blockIdx.x) * rag_gcache_cta_doubles();
   for (int c = 0; c < kRagClasses; ++c) {
@@ -938,7 +975,7 @@ __global__ void __launch_bounds__(kRagWarps * 32, 1)
         g.sync();
         if (item >= static_cast<unsigned long long>(rg.class_n[c])) break;
         const int64_t idx = static_cast<int64_t>(rg.order[rg.class_start[c] + static_cast<int64_t>(item)]);
-        rag_solve_system(rg, idx, g, ws, ld, gcache);
+        rag_solve_system(rg, idx, g, ws, ld, gcache, rag_w);
       }
       g.sync();
       if (g.t == 0) rag_mbar_inval(g.mbar);  // before the next phase reuses this memory

@@ -6,7 +6,9 @@
 // order through the arithmetic policy `Ops`, so the exact-mode kernels and the
 // CPU restatement evaluate the same rounded operations.  The first five are
 // the right-hand sides of the reference's own tests (src/ivp/rk.rs:664-670,
-// src/ivp/bdf.rs:769-783, src/ivp.rs:527-529).
+// src/ivp/bdf.rs:769-783, src/ivp.rs:527-529).  kAffine marks the ones affine
+// in y (f = J y + g(t) with J constant): with their exact Jacobian the
+// corrected BDF's Newton solve ends after its first update.
 #pragma once
 
 #include "device_math.cuh"
@@ -31,6 +33,7 @@ template <int D>
 struct RhsExp {  // y' = y
   static constexpr int DIM = D, NP = 0;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = true;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[D], const V*, V (&f)[D]) {
 #pragma unroll
@@ -42,6 +45,7 @@ template <int D>
 struct RhsDecay {  // y' = -y
   static constexpr int DIM = D, NP = 0;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = true;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[D], const V*, V (&f)[D]) {
 #pragma unroll
@@ -53,6 +57,7 @@ template <int D>
 struct RhsQuadratic {  // y' = -2 t
   static constexpr int DIM = D, NP = 0;
   static constexpr bool kUsesT = true;
+  static constexpr bool kAffine = true;
   template <class Ops>
   __device__ __forceinline__ static void eval(double t, const double (&)[D], const double*, double (&f)[D]) {
     const double v = Ops::mul(-2.0, t);
@@ -65,6 +70,7 @@ template <int D>
 struct RhsSine {  // y' = cos t
   static constexpr int DIM = D, NP = 0;
   static constexpr bool kUsesT = true;
+  static constexpr bool kAffine = true;
   template <class Ops>
   __device__ __forceinline__ static void eval(double t, const double (&)[D], const double*, double (&f)[D]) {
     const double v = cos(t);
@@ -76,6 +82,7 @@ struct RhsSine {  // y' = cos t
 struct RhsHarmonic {  // (y1, -y0)
   static constexpr int DIM = 2, NP = 0;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = true;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[2], const V*, V (&f)[2]) {
     f[0] = y[1];
@@ -86,6 +93,7 @@ struct RhsHarmonic {  // (y1, -y0)
 struct RhsVdp {  // y0' = y1, y1' = mu (1 - y0^2) y1 - y0
   static constexpr int DIM = 2, NP = 1;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = false;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[2], const V* p, V (&f)[2]) {
     f[0] = y[1];
@@ -96,6 +104,7 @@ struct RhsVdp {  // y0' = y1, y1' = mu (1 - y0^2) y1 - y0
 struct RhsLorenz {  // sigma (y1 - y0), y0 (rho - y2) - y1, y0 y1 - beta y2
   static constexpr int DIM = 3, NP = 3;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = false;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[3], const V* p, V (&f)[3]) {
     f[0] = Ops::mul(p[0], Ops::sub(y[1], y[0]));
@@ -107,6 +116,7 @@ struct RhsLorenz {  // sigma (y1 - y0), y0 (rho - y2) - y1, y0 y1 - beta y2
 struct RhsLotka {  // a x - b x y, c x y - d y
   static constexpr int DIM = 2, NP = 4;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = false;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[2], const V* p, V (&f)[2]) {
     f[0] = Ops::sub(Ops::mul(p[0], y[0]), Ops::mul(Ops::mul(p[1], y[0]), y[1]));
@@ -121,6 +131,7 @@ template <int N>
 struct RhsChain {
   static constexpr int DIM = 2 * N, NP = N + 1;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = true;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[2 * N], const V* p, V (&f)[2 * N]) {
     const V c = p[N];
@@ -331,6 +342,7 @@ struct Vjp<RhsLotka> {
 struct RhsRobertson {  // k1, k2, k3 kinetics
   static constexpr int DIM = 3, NP = 3;
   static constexpr bool kUsesT = false;
+  static constexpr bool kAffine = false;
   template <class Ops, class V>
   __device__ __forceinline__ static void eval(double, const V (&y)[3], const V* p, V (&f)[3]) {
     const V r1 = Ops::mul(p[0], y[0]);

@@ -164,8 +164,8 @@ def cpu_pool(fn, items, threads):
 
 
 def measured_peaks():
-    """The measured HBM and bf16 peaks of this GPU pool, or the
-    profiling recipe's fallback."""
+    """The measured HBM and bf16 peaks of these GPUs (MEASURED_PEAKS.json),
+    or fallback figures from an earlier GB300 measurement."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
@@ -435,9 +435,10 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
         "final_state_error_vs_rtol1e-12": {
             "robertson_vs_radau": A.final_state_error(us.y.cpu().numpy()[:, ri], rref),
             "chains_vs_expm_abs_max": cerr, "sample": "8 Robertson (Radau rtol 1e-12), 32 chains (exact expm)"},
-        "what": "corrected BDF6 (Newton, analytic Jacobian, partial-pivot LU) in one launch: Robertson one "
-                "system per thread, chains by warp groups with LU factors in shared memory and a 16-entry "
-                "factor cache per warp; bit-identical to the CPU restatement (tests/test_bdf_ragged_gpu.py)",
+        "what": "corrected BDF6 (Newton, analytic Jacobian, partial-pivot LU; one Newton update per solve for "
+                "the affine chains) in one launch: Robertson one system per thread, chains by warp groups with "
+                "LU factors in shared memory and a 16-entry factor cache per warp; bit-identical to the CPU "
+                "restatement (tests/test_bdf_ragged_gpu.py)",
         "_steps": {"robertson": (us.accepted.long() + us.rejected.long()).cpu().numpy(),
                    "chains": (rs.accepted.long() + rs.rejected.long()).cpu().numpy(), "dims": ch.dims}}
     return out

@@ -25,7 +25,9 @@
  * ORC_BDF_CORRECTED is this engine's stiff BDF (no reference counterpart to
  * follow beyond the structure above): orders 1..6 ramped up after every
  * restart, f at t_{n+1}, a true Newton iteration with the analytic Jacobian
- * (one partial-pivot LU per solve), and the reference's error estimate and
+ * (one partial-pivot LU per solve; for a right-hand side affine in y the
+ * first update solves the linear system, so the solve ends there, as
+ * ARKODE's linear-problem option does), and the reference's error estimate and
  * control — ||y_high - y_low||_2 <= tol, double dt below tol/10, halve on a
  * rejection — where y_low is the order-(q-1) solution with its own
  * coefficients.  After a doubling the history is re-sampled exactly (every
@@ -662,8 +664,18 @@ static void count_factorisation(int32_t rhs, double hb) {
   g_work[2]++;
 }
 
+/* Right-hand sides affine in y (f = J y + g(t), J constant): with their exact
+ * Jacobian G is linear, so the first Newton update lands on the solution up
+ * to the rounding of one LU solve. */
+static int rhs_affine(int32_t rhs) {
+  return rhs == ORC_RHS_EXP || rhs == ORC_RHS_DECAY || rhs == ORC_RHS_QUADRATIC || rhs == ORC_RHS_SINE ||
+         rhs == ORC_RHS_HARMONIC || rhs == ORC_RHS_CHAIN || rhs == ORC_RHS_LINEAR;
+}
+
 /* Solve G(y) = y - dt*b*f(t1, y) + sum_j a_j H[j-1] = 0 by Newton with the
- * Jacobian at the initial guess (one LU).  Returns 1 on convergence. */
+ * Jacobian at the initial guess (one LU).  Returns 1 on convergence: after
+ * the first update for an affine f (unless it is NaN), else once the update's
+ * norm is at most 1e-3 tol. */
 static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const double* p,
                             const double* shared, double t1, double dt, int q,
                             double H[][ORC_MAX_BDF_DIM], const double* guess0, double* y) {
@@ -698,6 +710,7 @@ static int corrected_newton(const oracle_bdf_cfg* cfg, int32_t rhs, int n, const
       dn = dn + (dx[d] * dx[d]);
     }
     if (!(dn == dn)) return 0;
+    if (rhs_affine(rhs)) return 1;
     if (sqrt(dn) <= 1e-3 * cfg->tol) return 1;
   }
   return 0;
