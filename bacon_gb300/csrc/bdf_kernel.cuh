@@ -114,6 +114,11 @@ __device__ __forceinline__ double bdf_norm(const double (&x)[D], bool dyn) {
   return O::sqrt(O::add(0.0, res));
 }
 
+// x == 0.0 (either sign) on the bit pattern, without an FP64 instruction.
+__device__ __forceinline__ bool bits_zero(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0ull;
+}
+
 // Newton solve of G(y) = y - h*b_q*f(t1, y) + sum_j a_{q,j} HH[j-1] = 0.
 template <class Rhs, int D>
 __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h, int q, const double (&HH)[7][D],
@@ -170,8 +175,11 @@ __device__ __forceinline__ bool bdf_newton(const double* p, double t1, double h,
     for (int r = i + 1; r < D; ++r) {
       const double l = O::mul(M[r][i], inv);
       M[r][i] = l;
+      // an exactly zero multiplier or pivot-row entry skips the update (the
+      // oracle's rule; the zero tests are integer operations)
 #pragma unroll
-      for (int k = i + 1; k < D; ++k) M[r][k] = __fma_rn(-l, M[i][k], M[r][k]);
+      for (int k = i + 1; k < D; ++k)
+        if (!bits_zero(l) && !bits_zero(M[i][k])) M[r][k] = __fma_rn(-l, M[i][k], M[r][k]);
     }
   }
   // rows of U scaled by their pivot reciprocal (a unit upper factor)

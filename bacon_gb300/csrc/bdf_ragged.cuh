@@ -374,35 +374,30 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
       // Trailing update, balanced over the whole group: columns dealt
       // round-robin to the warps, the m rows to the lanes (up to four each,
       // independent FMAs).  Every element receives the same FMA in the same
-      // pivot order as with one row per thread.
+      // pivot order as with one row per thread.  An update with an exactly
+      // zero multiplier or pivot-row entry is skipped (the oracle's rule):
+      // a zero U[i][k] skips the warp's column, a 32-row chunk without a
+      // nonzero multiplier is skipped by the whole warp, so the sparse
+      // factors of the chains cost a fraction of the dense update.
       const int w = r >> 5, lane = r & 31, nw = g.nthr >> 5;
       const double* lc = col + i + 1;
       const double l0 = lane < m ? lc[lane] : 0.0;
       const double l1 = lane + 32 < m ? lc[lane + 32] : 0.0;
       const double l2 = lane + 64 < m ? lc[lane + 64] : 0.0;
       const double l3 = lane + 96 < m ? lc[lane + 96] : 0.0;
-      int k = i + 1 + w;
-      for (; k + nw < D; k += 2 * nw) {  // two columns at a time, loads first
-        double* c0 = M + k * D + i + 1;
-        double* c1 = c0 + nw * D;
-        const double u0 = c0[-1], u1 = c1[-1];  // U[i][k], U[i][k + nw]
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0;
-        if (lane < m) { a0 = c0[lane]; b0 = c1[lane]; }
-        if (lane + 32 < m) { a1 = c0[lane + 32]; b1 = c1[lane + 32]; }
-        if (lane + 64 < m) { a2 = c0[lane + 64]; b2 = c1[lane + 64]; }
-        if (lane + 96 < m) { a3 = c0[lane + 96]; b3 = c1[lane + 96]; }
-        if (lane < m) { c0[lane] = __fma_rn(-l0, u0, a0); c1[lane] = __fma_rn(-l0, u1, b0); }
-        if (lane + 32 < m) { c0[lane + 32] = __fma_rn(-l1, u0, a1); c1[lane + 32] = __fma_rn(-l1, u1, b1); }
-        if (lane + 64 < m) { c0[lane + 64] = __fma_rn(-l2, u0, a2); c1[lane + 64] = __fma_rn(-l2, u1, b2); }
-        if (lane + 96 < m) { c0[lane + 96] = __fma_rn(-l3, u0, a3); c1[lane + 96] = __fma_rn(-l3, u1, b3); }
-      }
-      if (k < D) {
-        double* ck = M + k * D + i + 1;
-        const double u = ck[-1];
-        if (lane < m) ck[lane] = __fma_rn(-l0, u, ck[lane]);
-        if (lane + 32 < m) ck[lane + 32] = __fma_rn(-l1, u, ck[lane + 32]);
-        if (lane + 64 < m) ck[lane + 64] = __fma_rn(-l2, u, ck[lane + 64]);
-        if (lane + 96 < m) ck[lane + 96] = __fma_rn(-l3, u, ck[lane + 96]);
+      const bool n0 = !bits_zero(l0), n1 = !bits_zero(l1), n2 = !bits_zero(l2), n3 = !bits_zero(l3);
+      const bool g0 = __any_sync(0xffffffffu, n0), g1 = __any_sync(0xffffffffu, n1);
+      const bool g2 = __any_sync(0xffffffffu, n2), g3 = __any_sync(0xffffffffu, n3);
+      if (g0 || g1 || g2 || g3) {
+        for (int k = i + 1 + w; k < D; k += nw) {
+          double* ck = M + k * D + i + 1;
+          const double u = ck[-1];  // U[i][k], the same for the warp
+          if (bits_zero(u)) continue;
+          if (g0 && n0) ck[lane] = __fma_rn(-l0, u, ck[lane]);
+          if (g1 && n1) ck[lane + 32] = __fma_rn(-l1, u, ck[lane + 32]);
+          if (g2 && n2) ck[lane + 64] = __fma_rn(-l2, u, ck[lane + 64]);
+          if (g3 && n3) ck[lane + 96] = __fma_rn(-l3, u, ck[lane + 96]);
+        }
       }
     }
     g.sync();
@@ -416,8 +411,9 @@ __device__ __forceinline__ bool rag_factor(RagGroup& g, int D, int N, const doub
   // The diagonal 32-row blocks of L and of the scaled U replaced by their
   // inverses (strict parts in place): block b by warp b (its own rows), lane
   // c computing column c as the solve of e_c, every update taken for every
-  // column in the oracle's order.  The caller syncs before the factors are
-  // read.
+  // column in the oracle's order.  (Skipping the zero entries, a uniform test
+  // per update, measured slower: the unrolled FMAs cost less than the
+  // branches.)  The caller syncs before the factors are read.
   const int nw = g.nthr >> 5, lane = r & 31;
   for (int b = r >> 5; b * 32 < D; b += nw) {
     __syncwarp();

@@ -1607,12 +1607,27 @@ extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const 
   if (bacon_ctx_last_kernel_ms(c, &default_ms) != BACON_OK) return BACON_CUDA_ERROR;
   for (int v : variants) {
     c->force_variant = v;
+    const void* vfn = nullptr;
+    for (const auto& e : c->kernels)
+      if (e.key == key && e.variant == v) vfn = e.fn;
     const auto* shapes = v == 0 ? kShapes : kCappedShapes;
     const int ns = v == 0 ? static_cast<int>(sizeof(kShapes) / sizeof(kShapes[0]))
                           : static_cast<int>(sizeof(kCappedShapes) / sizeof(kCappedShapes[0]));
+    std::vector<std::pair<int, int>> timed;
     for (int k = 0; k < ns; ++k) {
+      // the shape as launched: CTAs per SM capped by this variant's occupancy,
+      // and a shape that caps onto one already timed is not timed again
+      int bps = shapes[k][1];
+      if (vfn) {
+        int max_bps = 0;
+        BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, vfn, shapes[k][0], 0));
+        if (max_bps >= 1 && bps > max_bps) bps = max_bps;
+      }
+      const std::pair<int, int> shape{shapes[k][0], bps};
+      if (std::find(timed.begin(), timed.end(), shape) != timed.end()) continue;
+      timed.push_back(shape);
       o.block = shapes[k][0];
-      o.blocks_per_sm = shapes[k][1];
+      o.blocks_per_sm = bps;
       rc = bacon_rk_solve(c, p, &o, r);
       if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
       double ms = 0.0;
@@ -1622,7 +1637,7 @@ extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const 
         best_ms = ms;
         bv = v;
         bb = shapes[k][0];
-        bs = shapes[k][1];
+        bs = bps;
       }
     }
   }

@@ -588,7 +588,13 @@ static int corrected_factor(int n, dmat M, int* piv, double* rinv) {
     for (int r = i + 1; r < n; ++r) {
       const double l = M[r][i] * inv;
       M[r][i] = l;
-      for (int k = i + 1; k < n; ++k) M[r][k] = fma(-l, M[i][k], M[r][k]);
+      /* An update with an exactly zero multiplier or pivot-row entry is
+       * skipped: it would only change the sign of a zero element.  The
+       * factors of the chains stay sparse (I - hb J of a banded J), so most
+       * updates are skipped. */
+      if (l == 0.0) continue;
+      for (int k = i + 1; k < n; ++k)
+        if (M[i][k] != 0.0) M[r][k] = fma(-l, M[i][k], M[r][k]);
     }
   }
   /* the rows of U scaled by their pivot reciprocal: the back substitution

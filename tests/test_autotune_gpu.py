@@ -26,7 +26,11 @@ def test_autotune_register_budget_variants_identical(engine):
     kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
     before = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
     t = engine.rk_autotune(b.y0, b.params, b.t0, b.t_end, details=True, **kw)
-    assert t["candidates"] == 8 + 2 * 4
+    # shapes that the occupancy caps onto one already timed are timed once,
+    # and the shape reported is the one launched
+    assert 8 <= t["candidates"] <= 8 + 2 * 4
+    if t["max_registers"]:
+        assert t["block"] * t["blocks_per_sm"] * t["max_registers"] <= 65536
     assert t["variant"] in (0, 1, 2) and t["max_registers"] in (0, 80, 64)
     assert t["best_ms"] <= t["default_ms"] * 1.05
     after = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
