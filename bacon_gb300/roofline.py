@@ -62,17 +62,19 @@ JAC_FLOPS = {8: 10, 9: 0}
 
 
 def bdf_flops(dim: int, rhs_flops: float, steps: float, newton_solves: float, newton_iters: float,
-              factorisations: float, jac_flops: float = 0.0, q: int = 6) -> float:
+              factorisations: float, jac_flops: float = 0.0, q: int = 6, lu_fraction: float = 1.0) -> float:
     """Corrected BDF: per step the predictor and the error norm; per Newton
     solve the Jacobian, the matrix I - h b_q J and the history constant; per
     Newton iteration the right-hand side, the residual, the two triangular
     substitutions (2 dim^2) and the update with its norm; per
-    factorisation the LU (2/3 dim^3) and the pivot reciprocals."""
+    factorisation the LU (2/3 dim^3 dense, times lu_fraction: the share of
+    its updates the elimination executes, since it skips updates by exactly
+    zero entries) and the pivot reciprocals."""
     n = float(dim)
     per_step = 2 * n * (q + 1) + 3 * n + 1
     per_solve = jac_flops + 2 * n * n + 2 * n * q
     per_iter = rhs_flops + 3 * n + 2 * n * n + 3 * n + 1
-    per_fact = 2.0 * n ** 3 / 3.0 + n
+    per_fact = lu_fraction * 2.0 * n ** 3 / 3.0 + n
     return steps * per_step + newton_solves * per_solve + newton_iters * per_iter + factorisations * per_fact
 
 

@@ -272,6 +272,8 @@ def stiff_work_model(work):
                        "iters_per_step": sum(w["newton_iters"] for w in ws) / steps,
                        "fact_per_step": sum(w["factorisations"] for w in ws) / steps,
                        "fact_per_system": sum(w["factorisations"] for w in ws) / len(ws),
+                       "lu_fraction": (sum(w["elim_fmas"] for w in ws) / sum(w["elim_fmas_dense"] for w in ws)
+                                       if sum(w["elim_fmas_dense"] for w in ws) else 1.0),
                        "systems": len(ws)}
     return rates
 
@@ -283,21 +285,23 @@ def stiff_roofline(R, rates, rob_steps, chain_dims, chain_steps, kernel_ms, fp64
     r0, r1 = rates[0], rates[1]
     steps = np.asarray(rob_steps, dtype=np.float64).sum()
     flops = R.bdf_flops(3, R.RHS_FLOPS[8], steps, r0["solves_per_step"] * steps, r0["iters_per_step"] * steps,
-                        r0["fact_per_step"] * steps, jac_flops=R.JAC_FLOPS[8])
+                        r0["fact_per_step"] * steps, jac_flops=R.JAC_FLOPS[8], lu_fraction=r0["lu_fraction"])
     dims = np.asarray(chain_dims, dtype=np.float64)
     cs = np.asarray(chain_steps, dtype=np.float64)
     for d in np.unique(dims):
         m = dims == d
         st = cs[m].sum()
         flops += R.bdf_flops(int(d), R.CHAIN_FLOPS_PER_COMPONENT * d, st, r1["solves_per_step"] * st,
-                             r1["iters_per_step"] * st, r1["fact_per_system"] * m.sum())
+                             r1["iters_per_step"] * st, r1["fact_per_system"] * m.sum(),
+                             lu_fraction=r1["lu_fraction"])
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     return {"bound": "fp64", "achieved": achieved, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
             "frac": achieved / fp64_peak_tflops, "traffic": None, "flops_per_launch": flops,
             "work": "model: GPU step counts per system x the CPU sample's Newton solves and iterations per step; "
                     "per Newton iteration rhs + 2 dim^2 substitutions + 6 dim, per solve I - h b J (2 dim^2), per "
-                    "factorisation 2/3 dim^3 (Robertson: every Newton solve; chains: one per distinct h b_q, "
-                    "sample mean per chain) (bacon_gb300/roofline.py bdf_flops)",
+                    "factorisation 2/3 dim^3 times the share of the dense updates the elimination executes (it "
+                    "skips updates by exact zeros; the CPU sample's ratio) (Robertson: every Newton solve; chains: "
+                    "one per distinct h b_q, sample mean per chain) (bacon_gb300/roofline.py bdf_flops)",
             "peak_source": "measured live (FP64 FMA probe kernel)"}
 
 

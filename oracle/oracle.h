@@ -154,10 +154,12 @@ int32_t oracle_bdf_solve_one(const oracle_bdf_cfg* cfg, int32_t rhs, int32_t dim
  * n x n, n <= 128) x = b.  Returns 1, or 0 on an exactly zero pivot. */
 int oracle_corrected_linsolve(int32_t n, const double* A, const double* b, double* x);
 /* Work of the corrected BDF on the calling thread since the last reset:
- * out3 = {Newton solves, Newton iterations, factorisations needed at the
+ * out5 = {Newton solves, Newton iterations, factorisations needed at the
  * least (one per distinct h*b_q of a solve for the constant-Jacobian chains,
- * one per Newton solve otherwise)}.  reset != 0 zeroes the counters. */
-void oracle_bdf_work(int64_t* out3, int reset);
+ * one per Newton solve otherwise), elimination FMAs executed (updates by an
+ * exactly zero entry skipped), elimination FMAs of the dense LU}.  reset != 0
+ * zeroes the counters. */
+void oracle_bdf_work(int64_t* out5, int reset);
 /* The inverse the as-compiled BDF's secant takes for a row-major n x n
  * matrix A: 1 partial-pivot LU, 2 full-pivot LU, 3 QR (src/ivp/bdf.rs:429-443),
  * 0 when all fail (SingularMatrix).  Test hook. */

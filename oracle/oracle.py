@@ -320,11 +320,13 @@ def bdf_secant_inverse(A):
 
 def bdf_work(reset: bool = True) -> dict:
     """Corrected-BDF work on the calling thread since the last reset:
-    Newton solves, Newton iterations and the factorisations needed at the
-    least (see oracle_bdf_work in oracle.h)."""
-    out = np.zeros(3, dtype=np.int64)
+    Newton solves, Newton iterations, the factorisations needed at the least,
+    and the elimination FMAs executed and of the dense LU (see
+    oracle_bdf_work in oracle.h)."""
+    out = np.zeros(5, dtype=np.int64)
     lib().oracle_bdf_work(out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(reset))
-    return {"newton_solves": int(out[0]), "newton_iters": int(out[1]), "factorisations": int(out[2])}
+    return {"newton_solves": int(out[0]), "newton_iters": int(out[1]), "factorisations": int(out[2]),
+            "elim_fmas": int(out[3]), "elim_fmas_dense": int(out[4])}
 
 
 # ---- Adams predictor-corrector and Euler (src/ivp/adams.rs, src/ivp.rs) ----
