@@ -715,7 +715,7 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
     fn = vfn;
   }
   const bool ff = opt->precision == BACON_FP32_COMP;
-  if (block == 0) block = ff ? 256 : 128;
+  if (block == 0) block = bacon::default_block(p->n, c->num_sms, ff ? 256 : 128);
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
@@ -1027,7 +1027,7 @@ extern "C" int bacon_bdf_solve(bacon_ctx* c, const bacon_problem* p, const bacon
   a.queue = c->d_ctl;
   a.first_fail = c->d_ctl + 1;
   int dyn = p->dyn_dim ? 1 : 0;
-  const int block = opt->block > 0 ? opt->block : 128;
+  const int block = opt->block > 0 ? opt->block : bacon::default_block(p->n, c->num_sms, 128);
   if (block % 32 != 0 || block > 128) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 128");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
@@ -1583,7 +1583,7 @@ extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const 
   // Launch shapes (threads per block, CTAs per SM) per register budget: the
   // default kernel over the whole range, the capped ones at the occupancies
   // their budgets open up.
-  static const int kShapes[][2] = {{64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}, {256, 3}};
+  static const int kShapes[][2] = {{32, 4}, {64, 2}, {128, 1}, {128, 2}, {128, 3}, {128, 4}, {256, 1}, {256, 2}};
   static const int kCappedShapes[][2] = {{128, 4}, {256, 2}, {256, 3}, {256, 4}};
   const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
   const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
@@ -1791,7 +1791,7 @@ extern "C" int bacon_rk_solve_adjoint(bacon_ctx* c, const bacon_problem* p, cons
     b.order = rev_oa.order;
   }
 
-  const int block = opt->block > 0 ? opt->block : 128;
+  const int block = opt->block > 0 ? opt->block : bacon::default_block(p->n, c->num_sms, 128);
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
   int fwd_bps = 0, rev_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fwd_bps, ent->fwd, block, 0));

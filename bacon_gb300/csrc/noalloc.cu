@@ -174,7 +174,7 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
     a.order = oa.order;
   }
 
-  const int block = opt->block > 0 ? opt->block : 128;
+  const int block = opt->block > 0 ? opt->block : bacon::default_block(p->n, num_sms, 128);
   if (block % 32 != 0 || block > 256) return BACON_INVALID_ARGUMENT;
   int max_bps = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0) != cudaSuccess || max_bps < 1)
