@@ -69,12 +69,15 @@ def bdf_flops(dim: int, rhs_flops: float, steps: float, newton_solves: float, ne
     substitutions (2 dim^2) and the update with its norm; per
     factorisation the LU (2/3 dim^3 dense, times lu_fraction: the share of
     its updates the elimination executes, since it skips updates by exactly
-    zero entries) and the pivot reciprocals."""
+    zero entries), the pivot reciprocals, and the inversion of the diagonal
+    32-row blocks of L and U (each column the solve of a unit vector over the
+    whole triangle: 2 nb^2 (nb - 1) flops per block of nb rows)."""
     n = float(dim)
     per_step = 2 * n * (q + 1) + 3 * n + 1
     per_solve = jac_flops + 2 * n * n + 2 * n * q
     per_iter = rhs_flops + 3 * n + 2 * n * n + 3 * n + 1
-    per_fact = lu_fraction * 2.0 * n ** 3 / 3.0 + n
+    blocks = [min(32, dim - s) for s in range(0, dim, 32)]
+    per_fact = lu_fraction * 2.0 * n ** 3 / 3.0 + n + sum(2.0 * nb * nb * (nb - 1) for nb in blocks)
     return steps * per_step + newton_solves * per_solve + newton_iters * per_iter + factorisations * per_fact
 
 

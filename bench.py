@@ -300,8 +300,9 @@ def stiff_roofline(R, rates, rob_steps, chain_dims, chain_steps, kernel_ms, fp64
             "work": "model: GPU step counts per system x the CPU sample's Newton solves and iterations per step; "
                     "per Newton iteration rhs + 2 dim^2 substitutions + 6 dim, per solve I - h b J (2 dim^2), per "
                     "factorisation 2/3 dim^3 times the share of the dense updates the elimination executes (it "
-                    "skips updates by exact zeros; the CPU sample's ratio) (Robertson: every Newton solve; chains: "
-                    "one per distinct h b_q, sample mean per chain) (bacon_gb300/roofline.py bdf_flops)",
+                    "skips updates by exact zeros; the CPU sample's ratio) plus the diagonal-block inversions "
+                    "(Robertson: every Newton solve; chains: one per distinct h b_q, sample mean per chain) "
+                    "(bacon_gb300/roofline.py bdf_flops)",
             "peak_source": "measured live (FP64 FMA probe kernel)"}
 
 
