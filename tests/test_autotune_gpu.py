@@ -13,7 +13,7 @@ def test_autotune_caches_and_keeps_results(engine):
     kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
     before = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
     block, bps = engine.rk_autotune(b.y0, b.params, b.t0, b.t_end, **kw)
-    assert block in (64, 128, 256) and 1 <= bps <= 4
+    assert block in (32, 64, 128, 256) and 1 <= bps <= 4
     after = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
     np.testing.assert_array_equal(after.y, before.y)
     np.testing.assert_array_equal(after.accepted, before.accepted)
