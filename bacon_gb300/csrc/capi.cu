@@ -448,16 +448,19 @@ int batch_return_code(bacon_ctx* c, const bacon_rk_result* r, bool host, const R
 namespace {
 
 // Lock-step batched RKF45 for y' = A y with a shared A (linear.cuh): one
-// round = one attempt for every running system = S stage GEMMs + one
-// control kernel; the host relaunches the round until no system runs.
+// round = one attempt for every running system = S GEMMs + one control
+// kernel; the host relaunches the round until no system runs.  The FP64
+// modes form the stage values K_i = dt A Y_i; the tensor-core mode forms the
+// products v_k = A^k y and the control kernel combines them (LinPoly).
 int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt, bacon_rk_result* r) {
   if (!p->shared) return fail(BACON_MISSING_PARAMETERS, "BACON_RHS_LINEAR needs the shared matrix");
   if (r->traj_t) return fail(BACON_UNSUPPORTED, "the linear engine records no trajectory");
   const bool tc = opt->precision == BACON_TC_SPLIT;
   bacon::LinKernels k;
   bacon::LinTcKernels tk;
-  // The tensor-core mode takes the FMA engine's control kernel: its stage
-  // values carry ~2^-36 relative error, far above a contraction's rounding.
+  // The tensor-core mode computes the products v_k = A^k y (one GEMM each)
+  // and combines them in its own control kernel, with FMA contraction: they
+  // carry ~2^-39 relative error, far above a contraction's rounding.
   if (!bacon::lin_kernels(opt->method, opt->layout, tc ? 1 : opt->precision, p->dim, k) ||
       (tc && !bacon::lin_tc_kernels(opt->method, opt->layout, p->dim, tk)))
     return fail(BACON_UNSUPPORTED, "linear engine: dim 64/128/256 (128/256 on tensor cores); layouts "
@@ -521,8 +524,9 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   const unsigned cg = static_cast<unsigned>((n * 32 + 255) / 256);
   const unsigned ctl_g = static_cast<unsigned>((n + bacon::kLinCtlSystemsPerBlock - 1) / bacon::kLinCtlSystemsPerBlock);
   const dim3 sg(static_cast<unsigned>((n + 63) / 64), static_cast<unsigned>(D / 64));
+  const void* control = tc ? tk.control : k.control;
   BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
-  BACON_CUDA(cudaLaunchKernel(k.control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
+  BACON_CUDA(cudaLaunchKernel(control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
   BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
   BACON_CUDA(cudaStreamSynchronize(c->stream));
   c->launches += 2;
@@ -545,6 +549,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     ta.ea = c->tc_ea.as<int32_t>();
     ta.sy = c->tc_sy.as<__nv_bfloat16>();
     ta.ey = c->tc_ey.as<int32_t>();
+    ta.unit_scale = 1;
     ta.error_flag = d_err;
     // about one second at the SM clock; the fault-injection hook withholds
     // the accumulator hand-off and shortens the waits to ~10 ms
@@ -568,9 +573,11 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   while (*h_live > 0) {
     for (int s = 0; s < k.stages; ++s) {
       if (tc) {
+        // v_{s+1} = A v_s into K[s], v_0 = y
         ta.stage = s;
-        void* slargs[] = {&ta, &sy, &ey};
-        BACON_CUDA(cudaLaunchKernel(tk.slice[s], dim3(cg), dim3(256), slargs, 0, c->stream));
+        const double* x = s == 0 ? st.y : st.K + static_cast<size_t>(s - 1) * n * D;
+        void* slargs[] = {&ta, &x, &sy, &ey};
+        BACON_CUDA(cudaLaunchKernel(tk.slice_vec, dim3(cg), dim3(256), slargs, 0, c->stream));
         void* gargs[] = {&ta};
         BACON_CUDA(cudaLaunchKernel(tk.gemm, tg, dim3(static_cast<unsigned>(tk.gemm_threads)), gargs,
                                     static_cast<size_t>(tk.smem_bytes), c->stream));
@@ -580,7 +587,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
       }
     }
     BACON_CUDA(cudaMemsetAsync(st.live, 0, sizeof(unsigned int), c->stream));
-    BACON_CUDA(cudaLaunchKernel(k.control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
+    BACON_CUDA(cudaLaunchKernel(control, dim3(ctl_g), dim3(bacon::kLinCtlThreads), cargs, 0, c->stream));
     BACON_CUDA(cudaMemcpyAsync(h_live, st.live, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     if (tc)  // a tensor-core stage that gave up a bounded wait ends the solve
       BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 3, c->d_ctl + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,

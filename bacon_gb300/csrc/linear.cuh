@@ -118,9 +118,59 @@ __global__ void __launch_bounds__(256) lin_stage_kernel(const LinArgs a) {
   }
 }
 
+// The tableau's stage polynomials for y' = A y.  With z = dt A the stage
+// inputs are Y_i = P_i(z) y, P_0 = 1, P_i = 1 + sum_{j<i} M(i,j) z P_j, and
+// the stage values K_j = z P_j(z) y.  So the attempt's update and error
+// vector are polynomials in z applied to y,
+//     sum_j b_j K_j = sum_{k=1..S} beta_k dt^k A^k y,
+//     sum_j e_j K_j = sum_{k=1..S} eps_k  dt^k A^k y,
+// and one attempt needs the S products v_k = A^k y = A v_{k-1}, whatever its
+// dt.  (For the fehlberg pair beta = 1, 1/2, 1/6, 1/24, 1/104, 0 and
+// eps = 0, 0, 0, 0, -1/780, 1/2080, up to the rounding of the quotients.)
+// Evaluated at compile time from the same IEEE quotients as the stage
+// kernels.
+template <class Tab>
+struct LinPoly {
+  static constexpr int S = Tab::S;
+  struct Coef {
+    double beta[S + 1];
+    double eps[S + 1];
+  };
+  static constexpr Coef make() {
+    double P[S][S] = {};  // P[i][k]: coefficient of z^k in P_i
+    for (int i = 0; i < S; ++i) {
+      P[i][0] = 1.0;
+      for (int j = 0; j < i; ++j)
+        for (int k = 0; k + 1 < S; ++k) P[i][k + 1] += Tab::M(i, j) * P[j][k];
+    }
+    Coef c{};
+    for (int j = 0; j < S; ++j)
+      for (int k = 0; k < S; ++k) {
+        c.beta[k + 1] += Tab::b(j) * P[j][k];
+        c.eps[k + 1] += Tab::e(j) * P[j][k];
+      }
+    return c;
+  }
+  static constexpr Coef kCoef = make();
+};
+
+// c[k-1] = beta_k dt^k (update) or eps_k dt^k (error), k = 1..S.
+template <class Tab, bool kBeta>
+__device__ __forceinline__ void lin_poly_scalars(double dt, double (&c)[Tab::S]) {
+  double p = dt;
+  static_for<0, Tab::S>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    constexpr double coef = kBeta ? LinPoly<Tab>::kCoef.beta[j + 1] : LinPoly<Tab>::kCoef.eps[j + 1];
+    c[j] = coef * p;
+    p = p * dt;
+  });
+}
+
 // Control kernel: finish the attempt in flight (error estimate, accept,
 // controller, dt_min check: rk.rs:386-416), then open the next one (Done /
-// attempt cap, end clamp: rk.rs:362-368).
+// attempt cap, end clamp: rk.rs:362-368).  With kPoly the attempt's vectors
+// are the products v_k = A^k y in K[k-1] (the tensor-core engine), combined
+// through LinPoly with the system's dt; otherwise they are the stage values.
 //
 // A warp serves kLinCtlGroup = 4 consecutive systems.  The element-wise
 // work (error vector, update of y) runs as full-warp passes over one system
@@ -134,7 +184,7 @@ constexpr int kLinCtlGroup = 4;    // systems per warp
 constexpr int kLinCtlThreads = 128;
 constexpr int kLinCtlSystemsPerBlock = kLinCtlGroup * kLinCtlThreads / 32;
 
-template <class Ops, class Tab, int D>
+template <class Ops, class Tab, int D, bool kPoly = false>
 __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinArgs a, int first) {
   static_assert(D >= 8 && D % 32 == 0, "dimension must be a multiple of 32");
   constexpr int S = Tab::S;
@@ -170,16 +220,26 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
 #pragma unroll
     for (int k = 0; k < G; ++k) {
       if (!run[k]) continue;  // whole warp
+      double eh[S];  // kPoly: eps_k dt^k for this system
+      if constexpr (kPoly) lin_poly_scalars<Tab, false>(a.dt[sys0 + k], eh);
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
         const int d = lane + 32 * q;
         const int64_t off = (sys0 + k) * D + d;
         double e = 0.0;
-        if constexpr (Tab::e(0) != 0.0) e = Ops::mul(a.K[off], Tab::e(0));
-        static_for<1, S>([&](auto jc) {
-          constexpr int j = decltype(jc)::value;
-          if constexpr (Tab::e(j) != 0.0) e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::e(j));
-        });
+        if constexpr (kPoly) {
+          static_for<0, S>([&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            if constexpr (LinPoly<Tab>::kCoef.eps[j + 1] != 0.0)
+              e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], eh[j]);
+          });
+        } else {
+          if constexpr (Tab::e(0) != 0.0) e = Ops::mul(a.K[off], Tab::e(0));
+          static_for<1, S>([&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            if constexpr (Tab::e(j) != 0.0) e = Ops::axpy(e, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::e(j));
+          });
+        }
         ev_s[w][k][d] = e;
       }
     }
@@ -229,13 +289,20 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
 #pragma unroll
     for (int k = 0; k < G; ++k) {
       if (!((upd_mask >> (8 * k)) & 1u)) continue;  // whole warp
+      double bh[S];  // kPoly: beta_k dt^k for this system
+      if constexpr (kPoly) lin_poly_scalars<Tab, true>(a.dt[sys0 + k], bh);
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
         const int64_t off = (sys0 + k) * D + lane + 32 * q;
         double v = a.y[off];
         static_for<0, S>([&](auto jc) {
           constexpr int j = decltype(jc)::value;
-          if constexpr (Tab::b(j) != 0.0) v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::b(j));
+          if constexpr (kPoly) {
+            if constexpr (LinPoly<Tab>::kCoef.beta[j + 1] != 0.0)
+              v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], bh[j]);
+          } else {
+            if constexpr (Tab::b(j) != 0.0) v = Ops::axpy(v, a.K[(static_cast<int64_t>(j) * n) * D + off], Tab::b(j));
+          }
         });
         a.y[off] = v;
       }

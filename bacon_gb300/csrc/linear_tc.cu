@@ -1,5 +1,6 @@
-// Instantiations of the tensor-core (split-precision) stage GEMM of the
-// linear engine.
+// Instantiations of the tensor-core (split-precision) engine for the linear
+// right-hand side: the GEMM, the slicing kernels and the control kernel that
+// combines the products A^k y.
 #include <cuda_bf16.h>
 
 #include "linear.h"
@@ -11,14 +12,8 @@ namespace {
 template <class Tab, int D>
 void fill_tc(LinTcKernels& k) {
   k.slice_a = reinterpret_cast<const void*>(&lin_tc_slice_a_kernel<D>);
-  k.slice[0] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 0>);
-  k.slice[1] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 1>);
-  k.slice[2] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 2>);
-  k.slice[3] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 3>);
-  if constexpr (Tab::S > 4) {
-    k.slice[4] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 4>);
-    k.slice[5] = reinterpret_cast<const void*>(&lin_tc_slice_kernel<Tab, D, 5>);
-  }
+  k.slice_vec = reinterpret_cast<const void*>(&lin_tc_slice_vec_kernel<D>);
+  k.control = reinterpret_cast<const void*>(&lin_control_kernel<FmaOps, Tab, D, true>);
   k.gemm = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D>);
   k.smem_bytes = 2 * kTcBufBytes;
   k.gemm_threads = kTcThreads;

@@ -87,6 +87,7 @@ struct TcArgs {
   const __nv_bfloat16* sy;  // slices of the stage inputs, chunk images (64-system tiles, padded)
   const int32_t* ey;        // [n]          system exponents
   int stage;
+  int unit_scale;           // 1: write A * Y_i (the products v_k), 0: dt * A * Y_i (the stage values)
   unsigned int* error_flag; // set when a bounded wait gives up
   long long wait_limit;     // SM clock cycles an mbarrier wait may take (about one second)
   int withhold_tmem_full;   // fault injection for tests: the producer never signals the epilogue
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
         const bool live = sys < n && a.st.status[sys] == kLinRunning;
         tile_live[tid] = live ? 1 : 0;
         tile_ey[tid] = live ? a.ey[sys] : 0;
-        tile_dt[tid] = live ? __double_as_longlong(a.st.dt[sys]) : 0ll;
+        tile_dt[tid] = live ? __double_as_longlong(a.unit_scale ? 1.0 : a.st.dt[sys]) : 0ll;
         const bool any = __any_sync(0xffffffffu, live);
         if (lane == 0) any_w[warp] = any ? 1 : 0;
       }
@@ -493,7 +494,7 @@ __device__ __forceinline__ unsigned long long tc_abs_bits(double x) {
   return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffull;
 }
 
-// Slices of the stage inputs Y_i = y + sum_j M(i,j) K_j, one warp per system.
+// Slices of a vector per system (the GEMM's B operand), one warp per system.
 // Lane l owns the PER = D/32 consecutive elements from PER*l: it loads them
 // as 16-byte vectors and writes each slice's PER bf16 values with one store
 // (16 bytes for D = 256, 8 for D = 128), since in a chunk image the K index
@@ -520,28 +521,14 @@ __device__ __forceinline__ void tc_load_run(const double* p, double (&v)[PER]) {
   }
 }
 
-template <class Tab, int D, int STAGE>
-__global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_bfloat16* sy, int32_t* ey) {
+// The system's exponent and the slices of its PER values from PER*lane (one
+// warp per system).
+template <int D>
+__device__ __forceinline__ void tc_slice_store(const double (&v)[D / 32], unsigned lane, int64_t sys,
+                                               __nv_bfloat16* sy, int32_t* ey) {
   constexpr int PER = D / 32;
   static_assert(PER == 4 || PER == 8, "vector stores of 8 or 16 bytes");
   using Vec = typename TcSliceVec<PER>::T;
-  const unsigned lane = threadIdx.x & 31u;
-  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
-  const int64_t n = a.st.n;
-  if (sys >= n || a.st.status[sys] != kLinRunning) return;
-  const int64_t off = sys * D + PER * lane;
-  double v[PER];
-  tc_load_run<PER>(a.st.y + off, v);
-  static_for<0, Tab::S>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    constexpr double m = Tab::M(STAGE, j);
-    if constexpr (m != 0.0) {
-      double kv[PER];
-      tc_load_run<PER>(a.st.K + (static_cast<int64_t>(j) * n) * D + off, kv);
-#pragma unroll
-      for (int i = 0; i < PER; ++i) v[i] = fma(kv[i], m, v[i]);
-    }
-  });
   unsigned long long mx = 0ull;
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
@@ -568,6 +555,20 @@ __global__ void __launch_bounds__(256) lin_tc_slice_kernel(const TcArgs a, __nv_
     for (int i = 0; i < PER; ++i) u.h[i] = qs[i][s];
     *reinterpret_cast<Vec*>(sy + tc_tile_index<D>(kTcN, sys, s, PER * static_cast<int>(lane))) = u.vec;
   }
+}
+
+// Slices of the vectors x (per system contiguous, [n][D]) of the running
+// systems: y, or the product v_k = A^k y for the next one.
+template <int D>
+__global__ void __launch_bounds__(256) lin_tc_slice_vec_kernel(const TcArgs a, const double* x, __nv_bfloat16* sy,
+                                                               int32_t* ey) {
+  constexpr int PER = D / 32;
+  const unsigned lane = threadIdx.x & 31u;
+  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  if (sys >= a.st.n || a.st.status[sys] != kLinRunning) return;
+  double v[PER];
+  tc_load_run<PER>(x + sys * D + PER * lane, v);
+  tc_slice_store<D>(v, lane, sys, sy, ey);
 }
 
 // Slices of A, one warp per row (computed once per solve).
