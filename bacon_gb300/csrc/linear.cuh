@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(256) lin_stage_kernel(const LinArgs a) {
 //     sum_j e_j K_j = sum_{k=1..S} eps_k  dt^k A^k y,
 // and one attempt needs the S products v_k = A^k y = A v_{k-1}, whatever its
 // dt.  (For the fehlberg pair beta = 1, 1/2, 1/6, 1/24, 1/104, 0 and
-// eps = 0, 0, 0, 0, -1/780, 1/2080, up to the rounding of the quotients.)
+// eps = 0, 0, 0, 0, -1/780, 1/2080, up to the rounding of the quotients; the
+// as_written matrix leaves eps_2..eps_4 nonzero.)
 // Evaluated at compile time from the same IEEE quotients as the stage
 // kernels.
 template <class Tab>
@@ -149,6 +150,13 @@ struct LinPoly {
         c.beta[k + 1] += Tab::b(j) * P[j][k];
         c.eps[k + 1] += Tab::e(j) * P[j][k];
       }
+    // A coefficient below 1e-15 in magnitude is the rounding residue of an
+    // exact zero (an order condition of the pair: eps_1..eps_4 of fehlberg
+    // come out near 1e-18); the genuine ones are above 1e-4.
+    for (int k = 0; k <= S; ++k) {
+      if (c.beta[k] < 1e-15 && c.beta[k] > -1e-15) c.beta[k] = 0.0;
+      if (c.eps[k] < 1e-15 && c.eps[k] > -1e-15) c.eps[k] = 0.0;
+    }
     return c;
   }
   static constexpr Coef kCoef = make();
