@@ -454,7 +454,6 @@ namespace {
 // products v_k = A^k y and the control kernel combines them (LinPoly).
 int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt, bacon_rk_result* r) {
   if (!p->shared) return fail(BACON_MISSING_PARAMETERS, "BACON_RHS_LINEAR needs the shared matrix");
-  if (r->traj_t) return fail(BACON_UNSUPPORTED, "the linear engine records no trajectory");
   const bool tc = opt->precision == BACON_TC_SPLIT;
   bacon::LinKernels k;
   bacon::LinTcKernels tk;
@@ -504,6 +503,14 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   st.dt_min = dt_min;
   st.dt_max = p->dt_max;
   st.max_attempts = opt->max_attempts > 0 ? opt->max_attempts : 10000000;
+  st.traj_t = o.traj_t;
+  st.traj_y = o.traj_y;
+  st.traj_cap = o.traj_t ? r->traj_cap : 0;
+  if (c->dense_off) {  // the second pass of bacon_rk_solve_dense
+    st.traj_t = c->dense_t;
+    st.traj_y = c->dense_y;
+    st.traj_off = c->dense_off;
+  }
   bacon::LinInitArgs ia{};
   ia.st = st;
   ia.dim = p->dim;
@@ -1553,7 +1560,6 @@ extern "C" int bacon_rk_solve_dense(bacon_ctx* c, const bacon_problem* p, const 
                                     bacon_rk_result* r, bacon_dense_output* dense) {
   NvtxRange nvtx_range("bacon_rk_solve_dense");
   if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
-  if (p->rhs == BACON_RHS_LINEAR) return fail(BACON_UNSUPPORTED, "the linear engine records no trajectory");
   return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_rk_solve(c, p, opt, r); });
 }
 

@@ -15,6 +15,7 @@
 #include "device_math.cuh"
 #include "rk_kernel.cuh"
 #include "tableau.cuh"
+#include "traj.cuh"
 
 namespace bacon {
 
@@ -35,6 +36,12 @@ struct LinArgs {
   unsigned int* live;  // systems running after the control kernel
   double tol, dt_min, dt_max;
   int64_t max_attempts;
+  // yielded items (t, y) of every accepted attempt, or NULL: a per-system
+  // slab of traj_cap items, or the packed stream with offsets traj_off
+  double* traj_t;
+  double* traj_y;
+  const int64_t* traj_off;
+  int32_t traj_cap;
 };
 
 // ---------------------------------------------------------------------------
@@ -222,6 +229,7 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
   }
   int32_t st = kLinRunning;
   int32_t acc_add = 0, rej_add = 0;
+  int64_t slot = -1;
 
   if (!first) {
     __shared__ double ev_s[kLinCtlThreads / 32][G][D];
@@ -276,8 +284,13 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
     else ndt = Ops::mul(dt, delta);
     if (ndt > a.dt_max) ndt = a.dt_max;
     bool upd = false;
+    // the slot of the item this attempt yields if accepted (before the
+    // accepted count is updated below)
+    if (a.traj_t != nullptr && mine) slot = traj_slot(a.traj_off, a.traj_cap, sys, a.accepted[sys]);
     if (ndt < a.dt_min && tn < end) {
       st = kStMinDt;
+    } else if (ok && a.traj_t != nullptr && slot < 0) {
+      st = kStCapacity;  // the trajectory is full: the item is not yielded
     } else if (ok) {
       upd = true;
       t = tn;
@@ -299,6 +312,10 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
       if (!((upd_mask >> (8 * k)) & 1u)) continue;  // whole warp
       double bh[S];  // kPoly: beta_k dt^k for this system
       if constexpr (kPoly) lin_poly_scalars<Tab, true>(a.dt[sys0 + k], bh);
+      // system k's item slot and new time, from its lanes 8k..8k+7
+      const long long slot_k = __shfl_sync(0xffffffffu, static_cast<long long>(slot), 8 * k);
+      const double t_k = __shfl_sync(0xffffffffu, t, 8 * k);
+      if (a.traj_t != nullptr && lane == 0) a.traj_t[slot_k] = t_k;
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
         const int64_t off = (sys0 + k) * D + lane + 32 * q;
@@ -313,6 +330,7 @@ __global__ void __launch_bounds__(kLinCtlThreads) lin_control_kernel(const LinAr
           }
         });
         a.y[off] = v;
+        if (a.traj_t != nullptr) a.traj_y[slot_k * D + lane + 32 * q] = v;
       }
     }
   }

@@ -442,8 +442,9 @@ typedef struct {
  * the per-system results filled and t / y untouched: allocate `total` items
  * and call again.  result->traj_t / traj_y must be NULL.  The fixed per-system
  * slabs of bacon_rk_result (traj_t, traj_cap) remain; a system whose slab is
- * full ends with BACON_CAPACITY_EXCEEDED instead of dropping items.  Not for
- * BACON_RHS_LINEAR. */
+ * full ends with BACON_CAPACITY_EXCEEDED instead of dropping items.  For
+ * BACON_RHS_LINEAR the items come from the lock-step engine's control kernel
+ * (every precision, BACON_TC_SPLIT included). */
 int bacon_rk_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_rk_options* options,
                          bacon_rk_result* result, bacon_dense_output* dense);
 int bacon_bdf_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, const bacon_bdf_options* options,

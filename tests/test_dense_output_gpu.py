@@ -168,3 +168,56 @@ def test_euler_dense_matches_oracle_path(engine, oracle):
     paths = [oracle.euler_solve_one(b.rhs, b.y0[:, i], 0.0, 2.0, 0.01, params=b.params[:, i], traj_cap=4096)
              for i in range(b.n)]
     _check_packed(sol, paths, 2)
+
+
+def test_linear_dense_exact_matches_oracle_paths(engine, oracle):
+    """The lock-step linear engine (one shared A, dim 64, FP64 exact) yields
+    every accepted (t, y) from its control kernel, bit-identical to the
+    oracle's per-system paths; per-system end times leave systems running in
+    different rounds."""
+    b = W.linear_shared(n=37, dim=64, seed=41)
+    t_end = np.random.default_rng(7).uniform(1.0, 5.0, b.n)
+    sol = engine.rk_solve(b.y0, None, 0.0, t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=2, precision=0, shared=b.extra["A"], dense=True)
+    assert sol.code == 0
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+    paths = [oracle.rk_solve_one(cfg, b.rhs, b.y0[:, i], 0.0, float(t_end[i]), shared=b.extra["A"],
+                                 traj_cap=4096) for i in range(b.n)]
+    _check_packed(sol, paths, 64)
+
+
+def test_linear_dense_tensor_core_path(engine):
+    """The tensor-core engine's items: one per accepted attempt, times
+    increasing to t_end, the last item the final state, and every state within
+    the split's accuracy of the exact solution at its own time."""
+    b = W.linear_shared(n=256, dim=128, seed=42)
+    sol = engine.rk_solve(b.y0, None, 0.0, 5.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=2, precision=engine.TC_SPLIT, shared=b.extra["A"], dense=True)
+    assert sol.code == 0
+    off = np.asarray(sol.traj_off)
+    assert np.all(np.diff(off) == sol.accepted)
+    q, lam = b.extra["Q"], b.extra["lambda"]
+    for i in range(0, b.n, 17):
+        a, e = int(off[i]), int(off[i + 1])
+        ts = sol.traj_t[a:e]
+        assert np.all(np.diff(ts) > 0) and ts[-1] == sol.t[i]
+        ys = sol.traj_y[a:e].reshape(-1, 128)
+        np.testing.assert_array_equal(ys[-1], sol.y[:, i])
+        exact = q @ (np.exp(-lam[:, None] * ts[None, :]) * (q.T @ b.y0[:, i])[:, None])
+        assert np.abs(ys - exact.T).max() < 1e-7
+
+
+def test_linear_slab_full_ends_with_capacity_status(engine, oracle):
+    """A per-system slab too small for the path: the system ends with
+    BACON_CAPACITY_EXCEEDED once the slab is full, its final state the last
+    item it yielded, as the oracle's path says."""
+    b = W.linear_shared(n=8, dim=64, seed=43)
+    sol = engine.rk_solve(b.y0, None, 0.0, 5.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                          layout=2, precision=0, shared=b.extra["A"], traj_cap=40)
+    assert (sol.status == 17).all() and (sol.accepted == 40).all() and sol.code == 17
+    cfg = oracle.rk_cfg(layout=2, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max)
+    for i in range(b.n):
+        p = oracle.rk_solve_one(cfg, b.rhs, b.y0[:, i], 0.0, 5.0, shared=b.extra["A"], traj_cap=4096)
+        np.testing.assert_array_equal(sol.traj_t[i], p.traj_t[:40])
+        np.testing.assert_array_equal(sol.traj_y[i].reshape(-1, 64), p.traj_y.reshape(-1, 64)[:40])
+        np.testing.assert_array_equal(sol.y[:, i], p.traj_y.reshape(-1, 64)[39])
