@@ -556,7 +556,6 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     ta.ea = c->tc_ea.as<int32_t>();
     ta.sy = c->tc_sy.as<__nv_bfloat16>();
     ta.ey = c->tc_ey.as<int32_t>();
-    ta.unit_scale = 1;
     ta.error_flag = d_err;
     // about one second at the SM clock; the fault-injection hook withholds
     // the accumulator hand-off and shortens the waits to ~10 ms

@@ -16,7 +16,8 @@
 // weigh at most 2^-24 of diagonal 0, so their rounding stays near 2^-40 of
 // the product.  Eight accumulators x 64 columns fill the 512 TMEM columns.
 // The epilogue combines them as 64-bit integers, applies 2^(e_row + e_sys)
-// and the system's dt, and writes K_i.  Pairs with s + t >= NS are dropped.
+// and writes the product: the engine forms v_k = A v_{k-1}.  Pairs with
+// s + t >= NS are dropped.
 // The relative error of the product is ~2^-39 (40-bit operands), with 15
 // slice products per K step; six 6-bit slices (exact sums in six
 // accumulators, 21 products) reached ~2^-35.
@@ -86,8 +87,7 @@ struct TcArgs {
   const int32_t* ea;        // [D]          row exponents of A
   const __nv_bfloat16* sy;  // slices of the stage inputs, chunk images (64-system tiles, padded)
   const int32_t* ey;        // [n]          system exponents
-  int stage;
-  int unit_scale;           // 1: write A * Y_i (the products v_k), 0: dt * A * Y_i (the stage values)
+  int stage;                // the product written: K[stage] = A * (the sliced vector)
   unsigned int* error_flag; // set when a bounded wait gives up
   long long wait_limit;     // SM clock cycles an mbarrier wait may take (about one second)
   int withhold_tmem_full;   // fault injection for tests: the producer never signals the epilogue
@@ -248,7 +248,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
   __shared__ int ok_sh;
   __shared__ int tile_live[kTcN];          // the tile's systems: running (and < n)
   __shared__ int tile_ey[kTcN];            // their exponents
-  __shared__ long long tile_dt[kTcN];      // the bits of their dt
 
   const int tid = threadIdx.x;
   const int warp = tid / 32;
@@ -392,7 +391,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
         const bool live = sys < n && a.st.status[sys] == kLinRunning;
         tile_live[tid] = live ? 1 : 0;
         tile_ey[tid] = live ? a.ey[sys] : 0;
-        tile_dt[tid] = live ? __double_as_longlong(a.unit_scale ? 1.0 : a.st.dt[sys]) : 0ll;
         const bool any = __any_sync(0xffffffffu, live);
         if (lane == 0) any_w[warp] = any ? 1 : 0;
       }
@@ -435,21 +433,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
         if (!tile_live[col]) continue;
         const int64_t sys = s0 + col;
         const int pe = erow + tile_ey[col] - kTcBits * (kTcSlices + 1);
-        const long long dtb = tile_dt[col];
-        const int dte = static_cast<int>((dtb >> 52) & 0x7ff);
         const double x = __ll2double_rn(acc[j]);
-        double k;
-        if (dte != 0 && dte != 0x7ff && dte + pe >= 1 && dte + pe <= 2046) {
-          // (x 2^pe) dt = x (2^pe dt): the power-of-two scaling of dt stays
-          // normal, so it is exact, and it is done on the exponent field
-          // (one product per element instead of two)
-          k = x * __longlong_as_double(dtb + static_cast<long long>(pe) * (1ll << 52));
-        } else {
-          const double p2 = (pe >= -1022 && pe <= 1023)
-                                ? __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
-                                : ldexp(1.0, pe);
-          k = (x * p2) * __longlong_as_double(dtb);
-        }
+        // x 2^pe: a product by a normal power of two, exact unless the result
+        // is subnormal; outside that exponent range ldexp rounds once
+        const double k = (pe >= -1022 && pe <= 1023)
+                             ? x * __longlong_as_double(static_cast<long long>(pe + 1023) << 52)
+                             : ldexp(x, pe);
         a.st.K[(static_cast<int64_t>(a.stage) * n + sys) * D + row] = k;
       }
     }
