@@ -551,6 +551,7 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     BACON_CUDA(cudaMemsetAsync(c->tc_sy.p, 0, sy_bytes, c->stream));
     BACON_CUDA(c->tc_ey.ensure(n * sizeof(int32_t)));
     BACON_CUDA(cudaFuncSetAttribute(tk.gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, tk.smem_bytes));
+    BACON_CUDA(cudaFuncSetAttribute(tk.gemm_last, cudaFuncAttributeMaxDynamicSharedMemorySize, tk.smem_bytes));
     ta.st = st;
     ta.sa = c->tc_sa.as<__nv_bfloat16>();
     ta.ea = c->tc_ea.as<int32_t>();
@@ -585,7 +586,8 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
         void* slargs[] = {&ta, &x, &sy, &ey};
         BACON_CUDA(cudaLaunchKernel(tk.slice_vec, dim3(cg), dim3(256), slargs, 0, c->stream));
         void* gargs[] = {&ta};
-        BACON_CUDA(cudaLaunchKernel(tk.gemm, tg, dim3(static_cast<unsigned>(tk.gemm_threads)), gargs,
+        BACON_CUDA(cudaLaunchKernel(s + 1 == k.stages ? tk.gemm_last : tk.gemm, tg,
+                                    dim3(static_cast<unsigned>(tk.gemm_threads)), gargs,
                                     static_cast<size_t>(tk.smem_bytes), c->stream));
         c->launches += 1;
       } else {

@@ -29,6 +29,8 @@ struct LinTcKernels {
   const void* slice_vec = nullptr; // __global__ void(TcArgs, const double* x, bf16* sy, int32_t* ey)
   const void* control = nullptr;   // __global__ void(LinArgs, int first)
   const void* gemm = nullptr;      // __global__ void(TcArgs)
+  const void* gemm_last = nullptr; // the GEMM for v_S (reduced precision when only the error uses it)
+  int last_pairs = 0;              // slice products of that GEMM
   int smem_bytes = 0;
   int gemm_threads = 0;
   int slices = 0;

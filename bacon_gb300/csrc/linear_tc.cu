@@ -15,6 +15,16 @@ void fill_tc(LinTcKernels& k) {
   k.slice_vec = reinterpret_cast<const void*>(&lin_tc_slice_vec_kernel<D>);
   k.control = reinterpret_cast<const void*>(&lin_control_kernel<FmaOps, Tab, D, true>);
   k.gemm = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D>);
+  // The last product enters only the error estimate when the update's
+  // polynomial has no term of degree S (fehlberg, as_written, BS23 alike):
+  // its leading two diagonals (~2^-15) suffice there.
+  if constexpr (LinPoly<Tab>::kCoef.beta[Tab::S] == 0.0) {
+    k.gemm_last = reinterpret_cast<const void*>(&lin_tc_stage_kernel<D, 2>);
+    k.last_pairs = 3;
+  } else {
+    k.gemm_last = k.gemm;
+    k.last_pairs = kTcSlices * (kTcSlices + 1) / 2;
+  }
   k.smem_bytes = 2 * kTcBufBytes;
   k.gemm_threads = kTcThreads;
   k.slices = kTcSlices;

@@ -196,11 +196,14 @@ __device__ __forceinline__ int64_t tc_tile_index(int rows, int64_t r, int s, int
 
 // One thread: announce a chunk's bytes on the buffer's mbarrier and start
 // its two bulk copies (sizes multiples of 16 bytes, addresses 16-byte
-// aligned).
+// aligned).  Only the leading kSl slices of each operand are copied (they
+// come first in a chunk image); the B part starts after room for all of A's.
+template <int kSl>
 __device__ __forceinline__ void tc_issue_chunk(uint32_t full_bar, unsigned char* dst, const __nv_bfloat16* srcA,
                                                const __nv_bfloat16* srcB) {
-  constexpr uint32_t kABytes = kTcSlices * kTcM * kTcKc * 2;
-  constexpr uint32_t kBBytes = kTcSlices * kTcN * kTcKc * 2;
+  constexpr uint32_t kABytes = kSl * kTcM * kTcKc * 2;
+  constexpr uint32_t kBBytes = kSl * kTcN * kTcKc * 2;
+  constexpr uint32_t kBOff = kTcSlices * kTcM * kTcKc * 2;
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full_bar), "r"(kABytes + kBBytes)
                : "memory");
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -208,7 +211,7 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t full_bar, unsigned char*
                "l"(srcA), "r"(kABytes), "r"(full_bar)
                : "memory");
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst + kABytes)),
+                   smem_addr(dst + kBOff)),
                "l"(srcB), "r"(kBBytes), "r"(full_bar)
                : "memory");
 }
@@ -231,8 +234,12 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
 
-template <int D>
+// kDiags: the leading diagonals s + t < kDiags of the slice products that
+// are formed (kTcSlices: all 15 pairs, ~2^-39; 2: the pairs (0,0), (0,1),
+// (1,0), ~2^-15, for a product that feeds only the error estimate).
+template <int D, int kDiags = kTcSlices>
 __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArgs a) {
+  static_assert(kDiags >= 1 && kDiags <= kTcSlices, "diagonals of the slice products");
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   constexpr int kABytes = kTcM * kTcKc * 2;  // 8192
   constexpr int kBBytes = kTcN * kTcKc * 2;  // 4096
@@ -306,7 +313,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
             pending[b] = false;
           }
           if (ok) {
-            tc_issue_chunk(smem_addr(&full_bar[b]), tc_smem + b * kTcBufBytes, srcA + c * kAChunk, srcB + c * kBChunk);
+            tc_issue_chunk<kDiags>(smem_addr(&full_bar[b]), tc_smem + b * kTcBufBytes, srcA + c * kAChunk,
+                                   srcB + c * kBChunk);
             inflight[b] = true;
           }
         };
@@ -340,9 +348,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
 #pragma unroll
             for (int ks = 0; ks < kTcKc / 16; ++ks) {
 #pragma unroll
-              for (int s = 0; s < kTcSlices; ++s) {
+              for (int s = 0; s < kDiags; ++s) {
 #pragma unroll
-                for (int t = 0; s + t < kTcSlices; ++t) {
+                for (int t = 0; s + t < kDiags; ++t) {
                   const int ac = tc_acc(s, t);
                   const uint64_t ad = a0 + static_cast<uint64_t>((s * kABytes + ks * 256) >> 4);
                   const uint64_t bd = b0 + static_cast<uint64_t>((t * kBBytes + ks * 256) >> 4);
@@ -412,6 +420,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
       for (int h = 0; h < 2; ++h) {
 #pragma unroll
         for (int ac = 0; ac < kTcAccs; ++ac) {
+          if (tc_acc_diag(ac) >= kDiags) continue;  // not formed (compile time)
           float v[16];
           tmem_ld16(tmem + (static_cast<uint32_t>(rw * 32) << 16) + static_cast<uint32_t>(ac * kTcN + cbase + 16 * h),
                     v);

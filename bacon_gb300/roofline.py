@@ -81,10 +81,13 @@ def bdf_flops(dim: int, rhs_flops: float, steps: float, newton_solves: float, ne
     return steps * per_step + newton_solves * per_solve + newton_iters * per_iter + factorisations * per_fact
 
 
-def linear_tc_flops(dim: int, attempts: int, stages: int = 6, slice_pairs: int = 15) -> tuple[float, float]:
-    """(bf16 tensor-core flops, FP64-equivalent flops) of the stage GEMMs of
-    the shared-matrix linear solve: every attempt of every system multiplies
-    its stage vector by A in each stage, as slice_pairs bf16 slice products
-    on the tensor cores, or one FP64 matrix-vector product of 2 dim^2."""
-    fp64 = float(attempts) * stages * 2.0 * dim * dim
-    return fp64 * slice_pairs, fp64
+def linear_tc_flops(dim: int, attempts: int, stages: int = 6, slice_pairs: int = 15,
+                    last_pairs: int | None = None) -> tuple[float, float]:
+    """(bf16 tensor-core flops, FP64-equivalent flops) of the GEMMs of the
+    shared-matrix linear solve: every attempt of every system multiplies a
+    vector by A `stages` times, as slice_pairs bf16 slice products on the
+    tensor cores (last_pairs for the last product, which feeds only the error
+    estimate), or one FP64 matrix-vector product of 2 dim^2."""
+    per = float(attempts) * 2.0 * dim * dim
+    lp = slice_pairs if last_pairs is None else last_pairs
+    return per * ((stages - 1) * slice_pairs + lp), per * stages

@@ -389,7 +389,8 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
     fp_s = time.perf_counter() - t0
     exact = lb.extra["exact"](5.0, slice(0, sub))
     att = int(tc.accepted.double().sum().item() + tc.rejected.double().sum().item())
-    bf16_fl, fp64_fl = R.linear_tc_flops(256, att)
+    # fehlberg: the sixth product enters only the error estimate (3 slice pairs)
+    bf16_fl, fp64_fl = R.linear_tc_flops(256, att, last_pairs=3)
     peaks = measured_peaks()
     bf16_ach = bf16_fl / tc_s / 1e12
     out["linear_shared_A_256"] = {
@@ -400,12 +401,15 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
                                       "unit": "TFLOP/s", "frac": bf16_ach / peaks["bf16_tflops"],
                                       "fp64_equivalent_tflops": fp64_fl / tc_s / 1e12,
                                       "peak_source": f"bf16 burst, {peaks['source']} (MEASURED_PEAKS.json)",
-                                      "work": "15 bf16 slice products of 2*256^2 per system, stage and attempt; "
-                                              "whole solve (stage GEMMs, slicing, control) in the time"}},
+                                      "work": "per system and attempt, the products A^k y, k = 1..6, each 15 "
+                                              "bf16 slice products of 2*256^2 (3 for A^6 y, which enters only "
+                                              "the error estimate); whole solve (GEMMs, slicing, control) in "
+                                              "the time"}},
         "fp64_fma": {"value": sub / fp_s, "unit": "solves/s", "n": sub,
                      "max_abs_err_vs_exact": float(np.abs(fp.y.cpu().numpy() - exact).max())},
-        "what": "lock-step RKF45 rounds; stage GEMM 256x256 x 256xN on tcgen05 (bf16 5x8-bit slices, FP32 "
-                "accumulation exact on the leading diagonals, ~2^-39 product error) vs FP64 DFMA SIMT GEMM; "
+        "what": "lock-step RKF45 rounds; GEMMs 256x256 x 256xN on tcgen05 forming A^k y (bf16 5x8-bit slices, "
+                "FP32 accumulation exact on the leading diagonals, ~2^-39 product error), combined per system "
+                "with its dt; vs the FP64 DFMA SIMT stage GEMM; "
                 "device time of the whole solve (CUDA events), error against the exact solution"}
 
     # Stiff batch, corrected BDF6, one launch: Robertson systems (a thread
