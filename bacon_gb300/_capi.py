@@ -162,6 +162,19 @@ class DenseOutput(ctypes.Structure):
     ]
 
 
+class RaggedDenseOutput(ctypes.Structure):
+    _fields_ = [
+        ("capacity", ctypes.c_int64),
+        ("value_capacity", ctypes.c_int64),
+        ("t", ctypes.c_void_p),
+        ("y", ctypes.c_void_p),
+        ("offsets", ctypes.c_void_p),
+        ("value_offsets", ctypes.c_void_p),
+        ("total", ctypes.c_int64),
+        ("total_values", ctypes.c_int64),
+    ]
+
+
 class Adjoint(ctypes.Structure):
     _fields_ = [
         ("target", ctypes.c_void_p),
@@ -218,6 +231,10 @@ SIGNATURES = {
                                                ctypes.POINTER(DenseOutput)]),
     "bacon_adams_solve_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(AdamsOptions),
                                                ctypes.POINTER(RkResult), ctypes.POINTER(DenseOutput)]),
+    "bacon_bdf_solve_mixed_dense": (ctypes.c_int, [_VP, ctypes.POINTER(Problem), ctypes.POINTER(RaggedProblem),
+                                                   ctypes.POINTER(BdfOptions), ctypes.POINTER(RkResult),
+                                                   ctypes.POINTER(RaggedResult), ctypes.POINTER(DenseOutput),
+                                                   ctypes.POINTER(RaggedDenseOutput)]),
     "bacon_rk_solve_noalloc": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(RkOptions),
                                               ctypes.POINTER(RkResult), _VP]),
     "bacon_builder_new": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)]),

@@ -205,6 +205,13 @@ struct RaggedArgs {
   unsigned long long* queues;  // [kRagClasses] work counters, zero at launch
   unsigned long long* first_fail;
   unsigned int* error_flag;    // raised when a bounded wait on a bulk copy gives up
+  // packed dense output, or null: system i's items (t, y) are the slots
+  // [traj_off[i], traj_off[i+1]) of traj_t, its values from traj_voff[i] of
+  // traj_y (item k at traj_voff[i] + k * dim_i)
+  double* traj_t;
+  double* traj_y;
+  const int64_t* traj_off;
+  const int64_t* traj_voff;
 };
 
 // Damped spring-mass chain (unit masses): rows 0..N-1 are x' = v, rows
@@ -875,7 +882,15 @@ __device__ __forceinline__ void rag_solve_system(const RaggedArgs& a, int64_t id
       g.sync();
       error = rag_norm_decide(g, D, sv, a.tol);
     }
+    if (ok && error <= a.tol && a.traj_t != nullptr && a.traj_off[idx] + acc >= a.traj_off[idx + 1]) {
+      status = kStCapacity;  // the dense output is full: the item is not yielded
+      break;
+    }
     if (ok && error <= a.tol) {
+      if (a.traj_t != nullptr) {
+        if (r == 0) a.traj_t[a.traj_off[idx] + acc] = t1;
+        if (own) a.traj_y[a.traj_voff[idx] + static_cast<int64_t>(acc) * D + r] = yh;
+      }
       const int kk = (k < 7) ? k + 1 : 7;
       g.sync();  // every row has finished reading H
       if (own) {

@@ -164,7 +164,14 @@ struct bacon_ctx {
   const int64_t* dense_off = nullptr;
   double* dense_t = nullptr;
   double* dense_y = nullptr;
+  // the same for the ragged part of bacon_bdf_solve_mixed: item offsets and
+  // value offsets (items x each system's dimension)
+  const int64_t* rg_dense_off = nullptr;
+  const int64_t* rg_dense_voff = nullptr;
+  double* rg_dense_t = nullptr;
+  double* rg_dense_y = nullptr;
   DevBuf dn_off, dn_t, dn_y;
+  DevBuf rdn_off, rdn_voff, rdn_t, rdn_y;
 };
 
 extern "C" {
@@ -212,7 +219,8 @@ int bacon_ctx_destroy(bacon_ctx* c) {
                     &c->adj_gy, &c->adj_gp, &c->lin_A, &c->lin_y, &c->lin_K, &c->lin_t, &c->lin_dt,
                     &c->lin_end, &c->lin_att, &c->tc_sa, &c->tc_ea, &c->tc_sy, &c->tc_ey, &c->rg_yoff,
                     &c->rg_poff, &c->rg_y0, &c->rg_p, &c->rg_t0, &c->rg_te, &c->rg_yout, &c->rg_tout,
-                    &c->rg_acc, &c->rg_rej, &c->rg_st, &c->rg_ord, &c->rg_lu, &c->dn_off, &c->dn_t, &c->dn_y})
+                    &c->rg_acc, &c->rg_rej, &c->rg_st, &c->rg_ord, &c->rg_lu, &c->dn_off, &c->dn_t, &c->dn_y,
+                    &c->rdn_off, &c->rdn_voff, &c->rdn_t, &c->rdn_y})
     b->release();
   if (c->ev2) cudaEventDestroy(c->ev2);
   if (c->ev3) cudaEventDestroy(c->ev3);
@@ -1327,6 +1335,11 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
     a.accepted = uo.acc;
     a.rejected = uo.rej;
     a.status = uo.st;
+    if (c->dense_off) {  // the second pass of bacon_bdf_solve_mixed_dense
+      a.traj_t = c->dense_t;
+      a.traj_y = c->dense_y;
+      a.traj_off = c->dense_off;
+    }
     dyn = up->dyn_dim ? 1 : 0;
   }
   a.max_steps = opt->max_steps > 0 ? opt->max_steps : 10000000;
@@ -1344,6 +1357,10 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
   rg.queues = c->d_ctl + 8;
   rg.first_fail = c->d_ctl + 5;
   rg.error_flag = reinterpret_cast<unsigned int*>(c->d_ctl + 6);
+  rg.traj_t = c->rg_dense_t;
+  rg.traj_y = c->rg_dense_y;
+  rg.traj_off = c->rg_dense_off;
+  rg.traj_voff = c->rg_dense_voff;
   for (int cl = 0, start = 0; cl < bacon::kRagClasses; start += static_cast<int>(class_n[cl]), ++cl) {
     rg.class_start[cl] = start;
     rg.class_n[cl] = class_n[cl];
@@ -1474,14 +1491,43 @@ extern "C" int bacon_bdf_solve_mixed(bacon_ctx* c, const bacon_problem* up, cons
 // first, writes each item straight to its slot.
 namespace {
 
-struct DenseGuard {  // clears the context's dense override on every exit
+struct DenseGuard {  // clears the context's dense overrides on every exit
   bacon_ctx* c;
   ~DenseGuard() {
     c->dense_off = nullptr;
     c->dense_t = nullptr;
     c->dense_y = nullptr;
+    c->rg_dense_off = nullptr;
+    c->rg_dense_voff = nullptr;
+    c->rg_dense_t = nullptr;
+    c->rg_dense_y = nullptr;
   }
 };
+
+// Copies n values between the caller's memory (host or device, as `host`
+// says) and a host vector.
+template <class T>
+int caller_to_host(bacon_ctx* c, bool host, T* dst, const T* src, size_t n) {
+  if (n == 0) return BACON_OK;
+  if (host) {
+    std::memcpy(dst, src, n * sizeof(T));
+    return BACON_OK;
+  }
+  BACON_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  return BACON_OK;
+}
+template <class T>
+int host_to_caller(bacon_ctx* c, bool host, T* dst, const T* src, size_t n) {
+  if (n == 0) return BACON_OK;
+  if (host) {
+    std::memcpy(dst, src, n * sizeof(T));
+    return BACON_OK;
+  }
+  BACON_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  BACON_CUDA(cudaStreamSynchronize(c->stream));
+  return BACON_OK;
+}
 
 template <class Solve>
 int dense_two_pass(bacon_ctx* c, const bacon_problem* p, int memory, bacon_rk_result* r, bacon_dense_output* dz,
@@ -1562,6 +1608,126 @@ extern "C" int bacon_rk_solve_dense(bacon_ctx* c, const bacon_problem* p, const 
   NvtxRange nvtx_range("bacon_rk_solve_dense");
   if (!opt || !p) return fail(BACON_INVALID_ARGUMENT, "NULL problem or options");
   return dense_two_pass(c, p, opt->memory, r, dense, [&]() { return bacon_rk_solve(c, p, opt, r); });
+}
+
+extern "C" int bacon_bdf_solve_mixed_dense(bacon_ctx* c, const bacon_problem* up, const bacon_ragged_problem* g,
+                                           const bacon_bdf_options* opt, bacon_rk_result* ur, bacon_ragged_result* gr,
+                                           bacon_dense_output* ud, bacon_ragged_dense_output* gd) {
+  NvtxRange nvtx_range("bacon_bdf_solve_mixed_dense");
+  if (!c || !opt) return fail(BACON_INVALID_ARGUMENT, "NULL context or options");
+  const bool host = opt->memory == BACON_MEM_HOST;
+  const int64_t un = up ? up->n : 0, gn = g ? g->n : 0;
+  if (!up) ud = nullptr;
+  if (!g) gd = nullptr;
+  if (ud) {
+    if (ud->capacity < 0) return fail(BACON_INVALID_ARGUMENT, "capacity < 0");
+    if (un > 0 && !ud->offsets) return fail(BACON_INVALID_ARGUMENT, "offsets is NULL");
+    if (ud->capacity > 0 && (!ud->t || !ud->y)) return fail(BACON_INVALID_ARGUMENT, "t or y is NULL");
+  }
+  if (gd) {
+    if (gd->capacity < 0 || gd->value_capacity < 0) return fail(BACON_INVALID_ARGUMENT, "capacity < 0");
+    if (gn > 0 && (!gd->offsets || !gd->value_offsets)) return fail(BACON_INVALID_ARGUMENT, "offsets is NULL");
+    if ((gd->capacity > 0 && !gd->t) || (gd->value_capacity > 0 && !gd->y))
+      return fail(BACON_INVALID_ARGUMENT, "t or y is NULL");
+  }
+  // Pass 1: the solve alone, for the per-system item counts.
+  int rc = bacon_bdf_solve_mixed(c, up, g, opt, ur, gr);
+  if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+  const std::string pass1_msg = g_last_error;
+  int rc0;
+  std::vector<int64_t> uoff, goff, gvoff;
+  if (ud) {
+    std::vector<int32_t> cnt(static_cast<size_t>(un));
+    if ((rc0 = caller_to_host(c, host, cnt.data(), ur->accepted, cnt.size())) != BACON_OK) return rc0;
+    uoff.assign(static_cast<size_t>(un) + 1, 0);
+    for (int64_t i = 0; i < un; ++i) uoff[i + 1] = uoff[i] + cnt[i];
+    ud->total = uoff[un];
+    if (un > 0 && (rc0 = host_to_caller(c, host, ud->offsets, uoff.data(), uoff.size())) != BACON_OK) return rc0;
+  }
+  if (gd) {
+    std::vector<int32_t> cnt(static_cast<size_t>(gn));
+    std::vector<int64_t> yo(static_cast<size_t>(gn) + 1);
+    if ((rc0 = caller_to_host(c, host, cnt.data(), gr->accepted, cnt.size())) != BACON_OK) return rc0;
+    if ((rc0 = caller_to_host(c, host, yo.data(), g->y_offsets, yo.size())) != BACON_OK) return rc0;
+    goff.assign(static_cast<size_t>(gn) + 1, 0);
+    gvoff.assign(static_cast<size_t>(gn) + 1, 0);
+    for (int64_t i = 0; i < gn; ++i) {
+      goff[i + 1] = goff[i] + cnt[i];
+      gvoff[i + 1] = gvoff[i] + static_cast<int64_t>(cnt[i]) * (yo[i + 1] - yo[i]);
+    }
+    gd->total = goff[gn];
+    gd->total_values = gvoff[gn];
+    if (gn > 0) {
+      if ((rc0 = host_to_caller(c, host, gd->offsets, goff.data(), goff.size())) != BACON_OK) return rc0;
+      if ((rc0 = host_to_caller(c, host, gd->value_offsets, gvoff.data(), gvoff.size())) != BACON_OK) return rc0;
+    }
+  }
+  if (ud && ud->total > ud->capacity)
+    return fail(BACON_CAPACITY_EXCEEDED, "dense output of the uniform part needs " + std::to_string(ud->total) +
+                                             " items, capacity is " + std::to_string(ud->capacity));
+  if (gd && (gd->total > gd->capacity || gd->total_values > gd->value_capacity))
+    return fail(BACON_CAPACITY_EXCEEDED, "dense output of the ragged part needs " + std::to_string(gd->total) +
+                                             " items and " + std::to_string(gd->total_values) + " values");
+  const int64_t utot = ud ? ud->total : 0, gtot = gd ? gd->total : 0, gvtot = gd ? gd->total_values : 0;
+  if (utot == 0 && gtot == 0) {
+    g_last_error = pass1_msg;
+    return rc;
+  }
+  // Pass 2: the same solve, writing every item to its packed slot.
+  DenseGuard guard{c};
+  const int dim = up ? up->dim : 0;
+  if (utot > 0) {
+    if (host) {
+      BACON_CUDA(c->dn_off.ensure(uoff.size() * sizeof(int64_t)));
+      BACON_CUDA(c->dn_t.ensure(static_cast<size_t>(utot) * sizeof(double)));
+      BACON_CUDA(c->dn_y.ensure(static_cast<size_t>(utot) * dim * sizeof(double)));
+      BACON_CUDA(cudaMemcpyAsync(c->dn_off.p, uoff.data(), uoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                 c->stream));
+      c->dense_off = c->dn_off.as<int64_t>();
+      c->dense_t = c->dn_t.as<double>();
+      c->dense_y = c->dn_y.as<double>();
+    } else {
+      c->dense_off = ud->offsets;
+      c->dense_t = ud->t;
+      c->dense_y = ud->y;
+    }
+  }
+  if (gtot > 0) {
+    if (host) {
+      BACON_CUDA(c->rdn_off.ensure(goff.size() * sizeof(int64_t)));
+      BACON_CUDA(c->rdn_voff.ensure(gvoff.size() * sizeof(int64_t)));
+      BACON_CUDA(c->rdn_t.ensure(static_cast<size_t>(gtot) * sizeof(double)));
+      BACON_CUDA(c->rdn_y.ensure(static_cast<size_t>(gvtot) * sizeof(double)));
+      BACON_CUDA(cudaMemcpyAsync(c->rdn_off.p, goff.data(), goff.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                 c->stream));
+      BACON_CUDA(cudaMemcpyAsync(c->rdn_voff.p, gvoff.data(), gvoff.size() * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, c->stream));
+      c->rg_dense_off = c->rdn_off.as<int64_t>();
+      c->rg_dense_voff = c->rdn_voff.as<int64_t>();
+      c->rg_dense_t = c->rdn_t.as<double>();
+      c->rg_dense_y = c->rdn_y.as<double>();
+    } else {
+      c->rg_dense_off = gd->offsets;
+      c->rg_dense_voff = gd->value_offsets;
+      c->rg_dense_t = gd->t;
+      c->rg_dense_y = gd->y;
+    }
+  }
+  const int rc2 = bacon_bdf_solve_mixed(c, up, g, opt, ur, gr);
+  if (rc2 == BACON_CUDA_ERROR || rc2 == BACON_INVALID_ARGUMENT || rc2 == BACON_UNSUPPORTED) return rc2;
+  if (rc2 != rc) return fail(BACON_CUDA_ERROR, "dense output: the second pass ended differently from the first");
+  if (host) {
+    if (utot > 0) {
+      BACON_CUDA(cudaMemcpyAsync(ud->t, c->dense_t, utot * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      BACON_CUDA(cudaMemcpyAsync(ud->y, c->dense_y, utot * dim * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (gtot > 0) {
+      BACON_CUDA(cudaMemcpyAsync(gd->t, c->rg_dense_t, gtot * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      BACON_CUDA(cudaMemcpyAsync(gd->y, c->rg_dense_y, gvtot * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    BACON_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return rc2;
 }
 
 extern "C" int bacon_bdf_solve_dense(bacon_ctx* c, const bacon_problem* p, const bacon_bdf_options* opt,

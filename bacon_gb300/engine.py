@@ -416,6 +416,10 @@ class RaggedSolution:
     rejected: Any
     status: Any
     code: int
+    traj_t: Any = None     # dense output: system i's items are [traj_off[i], traj_off[i+1])
+    traj_y: Any = None     # flat: its states from traj_voff[i], dim_i values each
+    traj_off: Any = None
+    traj_voff: Any = None
 
 
 def _alloc_ragged(total: int, n: int, device: bool):
@@ -433,13 +437,14 @@ def _alloc_ragged(total: int, n: int, device: bool):
 
 def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_steps=0,
                     ctx: Context | None = None, blocks_per_sm=0, uniform_out=None, ragged_out=None,
-                    raise_on_error=False):
+                    raise_on_error=False, dense=False):
     """One launch of the corrected BDF over a stiff batch of a uniform part
     (attributes y0 (dim, n), params, t0, t_end, rhs, tol, dt_min, dt_max, as
     workloads.Batch) and a ragged part (y_off, p_off, flat y0 and params, t0,
     t_end, rhs, tol, dt_min, dt_max, as workloads.RaggedBatch).  Arrays are
     all numpy (host) or all CUDA tensors.  Returns (Solution | None,
-    RaggedSolution | None)."""
+    RaggedSolution | None).  ``dense``: every yielded item of both parts,
+    packed (bacon_bdf_solve_mixed_dense), in the solutions' traj_* fields."""
     ctx = ctx or default_context()
     first = uniform.y0 if uniform is not None else ragged.y0
     device = _is_device(first)
@@ -476,19 +481,72 @@ def bdf_solve_mixed(uniform=None, ragged=None, *, method=BDF6, max_iter=0, max_s
         rres = _capi.RaggedResult()
         rres.y_final, rres.t_final = _ptr(rout["y"]), _ptr(rout["t"])
         rres.accepted, rres.rejected, rres.status = _ptr(rout["accepted"]), _ptr(rout["rejected"]), _ptr(rout["status"])
-    code = _capi.load().bacon_bdf_solve_mixed(ctx.handle, ctypes.byref(prob) if prob is not None else None,
-                                              ctypes.byref(rp) if rp is not None else None, ctypes.byref(o),
-                                              ctypes.byref(ures) if ures is not None else None,
-                                              ctypes.byref(rres) if rres is not None else None)
+    args = (ctx.handle, ctypes.byref(prob) if prob is not None else None,
+            ctypes.byref(rp) if rp is not None else None, ctypes.byref(o),
+            ctypes.byref(ures) if ures is not None else None, ctypes.byref(rres) if rres is not None else None)
+    udz = gdz = None
+    if dense:
+        code, udz, gdz = _mixed_dense_call(args, uniform, ragged, device)
+    else:
+        code = _capi.load().bacon_bdf_solve_mixed(*args)
     if code in (14, 15, 16) or (raise_on_error and code != 0):
         raise IVPError(code, _capi.last_error())
     us = None
     if uout is not None:
         us = Solution(uout["y"], uout["t"], uout["accepted"], uout["rejected"], uout["status"], int(code))
+        if udz is not None:
+            us.traj_t, us.traj_y, us.traj_off = udz
     rs = None
     if rout is not None:
         rs = RaggedSolution(rout["y"], rout["t"], rout["accepted"], rout["rejected"], rout["status"], int(code))
+        if gdz is not None:
+            rs.traj_t, rs.traj_y, rs.traj_off, rs.traj_voff = gdz
     return us, rs
+
+
+def _mixed_dense_call(args, uniform, ragged, device):
+    """bacon_bdf_solve_mixed_dense: the item counts first (capacity 0), then
+    the solve into arrays of exactly that size.  Returns (code, uniform
+    (t, y, offsets) or None, ragged (t, y, offsets, value offsets) or None)."""
+    if device:
+        import torch
+        dev = torch.device("cuda")
+        mk = lambda shape, dt: torch.empty(shape, dtype=dt, device=dev)  # noqa: E731
+        f64, i64 = torch.float64, torch.int64
+    else:
+        mk = lambda shape, dt: np.empty(shape, dtype=dt)  # noqa: E731
+        f64, i64 = np.float64, np.int64
+    udz = gdz = None
+    uoff = goff = gvoff = None
+    if uniform is not None:
+        dim, n = int(uniform.y0.shape[0]), int(uniform.y0.shape[1])
+        uoff = mk(n + 1, i64)
+        udz = _capi.DenseOutput()
+        udz.capacity, udz.t, udz.y, udz.offsets = 0, None, None, _ptr(uoff)
+    if ragged is not None:
+        gn = int(ragged.y_off.shape[0]) - 1
+        goff, gvoff = mk(gn + 1, i64), mk(gn + 1, i64)
+        gdz = _capi.RaggedDenseOutput()
+        gdz.capacity, gdz.value_capacity, gdz.t, gdz.y = 0, 0, None, None
+        gdz.offsets, gdz.value_offsets = _ptr(goff), _ptr(gvoff)
+    fn = _capi.load().bacon_bdf_solve_mixed_dense
+    by = lambda x: ctypes.byref(x) if x is not None else None  # noqa: E731
+    code = fn(*args, by(udz), by(gdz))
+    if code in (14, 15, 16):
+        raise IVPError(code, _capi.last_error())
+    ut = uy = gt = gy = None
+    if udz is not None:
+        cap = int(udz.total)
+        ut, uy = mk(max(cap, 1), f64), mk((max(cap, 1), dim), f64)
+        udz.capacity, udz.t, udz.y = cap, _ptr(ut), _ptr(uy)
+    if gdz is not None:
+        cap, vcap = int(gdz.total), int(gdz.total_values)
+        gt, gy = mk(max(cap, 1), f64), mk(max(vcap, 1), f64)
+        gdz.capacity, gdz.value_capacity, gdz.t, gdz.y = cap, vcap, _ptr(gt), _ptr(gy)
+    code = fn(*args, by(udz), by(gdz))
+    u = (ut[:int(udz.total)], uy[:int(udz.total)], uoff) if udz is not None else None
+    g = (gt[:int(gdz.total)], gy[:int(gdz.total_values)], goff, gvoff) if gdz is not None else None
+    return code, u, g
 
 
 def adams_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, order=5, max_attempts=0, traj_cap=0,

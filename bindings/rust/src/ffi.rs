@@ -177,6 +177,19 @@ pub struct bacon_dense_output {
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug)]
+pub struct bacon_ragged_dense_output {
+    pub capacity: i64,
+    pub value_capacity: i64,
+    pub t: *mut f64,
+    pub y: *mut f64,
+    pub offsets: *mut i64,
+    pub value_offsets: *mut i64,
+    pub total: i64,
+    pub total_values: i64,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
 pub struct bacon_adjoint {
     pub target: *const f64,
     pub loss: *mut f64,
@@ -277,6 +290,16 @@ extern "C" {
         options: *const bacon_rk_options,
         result: *mut bacon_rk_result,
         dense: *mut bacon_dense_output,
+    ) -> c_int;
+    pub fn bacon_bdf_solve_mixed_dense(
+        ctx: *mut bacon_ctx,
+        uniform: *const bacon_problem,
+        ragged: *const bacon_ragged_problem,
+        options: *const bacon_bdf_options,
+        uniform_result: *mut bacon_rk_result,
+        ragged_result: *mut bacon_ragged_result,
+        uniform_dense: *mut bacon_dense_output,
+        ragged_dense: *mut bacon_ragged_dense_output,
     ) -> c_int;
     pub fn bacon_bdf_solve_dense(
         ctx: *mut bacon_ctx,

@@ -455,6 +455,31 @@ int bacon_euler_solve_dense(bacon_ctx* ctx, const bacon_problem* problem, double
                             const bacon_adams_options* options, bacon_rk_result* result,
                             bacon_dense_output* dense);
 
+/* Dense output of the ragged part of a mixed batch: system i's items are
+ * t[offsets[i] .. offsets[i+1]) and its states, dim_i values each, are
+ * y[value_offsets[i] .. value_offsets[i+1]) (item k from
+ * value_offsets[i] + k * dim_i).  Memory kind as the batch. */
+typedef struct {
+  int64_t capacity;        /* items t can hold */
+  int64_t value_capacity;  /* doubles y can hold */
+  double* t;               /* [capacity] */
+  double* y;               /* [value_capacity] */
+  int64_t* offsets;        /* [n+1], written by the call */
+  int64_t* value_offsets;  /* [n+1], written by the call */
+  int64_t total;           /* out: items of the ragged part */
+  int64_t total_values;    /* out: doubles of the ragged part */
+} bacon_ragged_dense_output;
+
+/* bacon_bdf_solve_mixed with dense output, in the same two passes as
+ * bacon_rk_solve_dense.  uniform_dense / ragged_dense may be NULL: that
+ * part's items are then not recorded.  BACON_CAPACITY_EXCEEDED after the
+ * first pass, with the totals and offsets filled, when either part's
+ * capacity is short. */
+int bacon_bdf_solve_mixed_dense(bacon_ctx* ctx, const bacon_problem* uniform, const bacon_ragged_problem* ragged,
+                                const bacon_bdf_options* options, bacon_rk_result* uniform_result,
+                                bacon_ragged_result* ragged_result, bacon_dense_output* uniform_dense,
+                                bacon_ragged_dense_output* ragged_dense);
+
 /* ---- discrete adjoint ---------------------------------------------------- */
 /* Gradient of L_i = sum_d (y_i(T)[d] - target_i[d])^2 for every system i with
  * respect to its initial state and parameters, through the accepted-step

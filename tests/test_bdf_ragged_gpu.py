@@ -121,3 +121,72 @@ def test_ragged_failures_retire_only_their_system(engine, oracle):
     assert sol.status[0] == 0 and sol.status[1] == 5 and sol.status[2] != 0
     np.testing.assert_array_equal(sol.status, ref["status"])
     assert sol.code == 5
+
+
+def test_mixed_dense_output_matches_oracle_paths(engine, oracle):
+    """bacon_bdf_solve_mixed_dense: every item of both parts, packed.  The
+    ragged chains' states go to one flat stream with value offsets (items x
+    each chain's own dimension); chains and Robertson systems match the
+    oracle's per-system paths bit for bit, and the final states equal the
+    plain mixed solve's."""
+    r = _chains(MASSES, seed=35, t_end=0.3)
+    rob = W.robertson(n=48, seed=36)
+    rob.t_end = np.full(rob.n, 10.0)
+    us, rs = engine.bdf_solve_mixed(rob, r, dense=True)
+    assert us.code == 0 and rs.code == 0
+    off, voff = np.asarray(rs.traj_off), np.asarray(rs.traj_voff)
+    dims = np.diff(r.y_off)
+    np.testing.assert_array_equal(np.diff(off), rs.accepted)
+    np.testing.assert_array_equal(np.diff(voff), rs.accepted * dims)
+    cfg = oracle.bdf_cfg(mode=oracle.BDF_CORRECTED, dyn_dim=True, tol=r.tol, dt_min=r.dt_min, dt_max=r.dt_max)
+    for i in range(r.n):
+        y0, p = r.system(i)
+        path = oracle.bdf_solve_one(cfg, r.rhs, y0, r.t0[i], r.t_end[i], params=p, traj_cap=100000)
+        a, b = int(off[i]), int(off[i + 1])
+        assert b - a == path.accepted
+        np.testing.assert_array_equal(rs.traj_t[a:b], path.traj_t)
+        np.testing.assert_array_equal(rs.traj_y[voff[i]:voff[i + 1]], path.traj_y.reshape(-1))
+    rcfg = oracle.bdf_cfg(mode=oracle.BDF_CORRECTED, tol=rob.tol, dt_min=rob.dt_min, dt_max=rob.dt_max)
+    uoff = np.asarray(us.traj_off)
+    for i in range(0, rob.n, 5):
+        path = oracle.bdf_solve_one(rcfg, rob.rhs, rob.y0[:, i], 0.0, 10.0, params=rob.params[:, i],
+                                    traj_cap=100000)
+        a, b = int(uoff[i]), int(uoff[i + 1])
+        np.testing.assert_array_equal(us.traj_t[a:b], path.traj_t)
+        np.testing.assert_array_equal(us.traj_y[a:b].reshape(-1), path.traj_y.reshape(-1))
+    plain_u, plain_r = engine.bdf_solve_mixed(rob, r)
+    np.testing.assert_array_equal(plain_r.y, rs.y)
+    np.testing.assert_array_equal(plain_u.y, us.y)
+
+
+def test_mixed_dense_capacity_short_reports_totals(engine):
+    """With capacity 0 the call returns BACON_CAPACITY_EXCEEDED after the
+    counting pass, with both totals and the offsets filled."""
+    import ctypes
+    from bacon_gb300 import _capi
+    r = _chains([2, 5, 17], seed=37, t_end=0.2)
+    rp = _capi.RaggedProblem()
+    rp.n, rp.rhs = r.n, int(r.rhs)
+    y_off, p_off = np.ascontiguousarray(r.y_off), np.ascontiguousarray(r.p_off)
+    y0, prm = np.ascontiguousarray(r.y0), np.ascontiguousarray(r.params)
+    t0, te = np.ascontiguousarray(r.t0), np.ascontiguousarray(r.t_end)
+    rp.y_offsets, rp.p_offsets, rp.y0, rp.params = y_off.ctypes.data, p_off.ctypes.data, y0.ctypes.data, prm.ctypes.data
+    rp.t0, rp.t_end = t0.ctypes.data, te.ctypes.data
+    rp.tol, rp.dt_min, rp.dt_max = r.tol, r.dt_min, r.dt_max
+    o = _capi.BdfOptions()
+    o.method, o.mode, o.memory = 0, 1, 1
+    yf, tf = np.zeros_like(y0), np.zeros(r.n)
+    acc, rej, st = np.zeros(r.n, np.int32), np.zeros(r.n, np.int32), np.zeros(r.n, np.int32)
+    rres = _capi.RaggedResult()
+    rres.y_final, rres.t_final = yf.ctypes.data, tf.ctypes.data
+    rres.accepted, rres.rejected, rres.status = acc.ctypes.data, rej.ctypes.data, st.ctypes.data
+    off, voff = np.zeros(r.n + 1, np.int64), np.zeros(r.n + 1, np.int64)
+    gd = _capi.RaggedDenseOutput()
+    gd.capacity, gd.value_capacity, gd.t, gd.y = 0, 0, None, None
+    gd.offsets, gd.value_offsets = off.ctypes.data, voff.ctypes.data
+    code = _capi.load().bacon_bdf_solve_mixed_dense(engine.default_context().handle, None, ctypes.byref(rp),
+                                                    ctypes.byref(o), None, ctypes.byref(rres), None,
+                                                    ctypes.byref(gd))
+    assert code == 17
+    assert gd.total == acc.sum() == off[-1] > 0
+    assert gd.total_values == (acc * np.diff(y_off)).sum() == voff[-1]
