@@ -190,3 +190,24 @@ def test_mixed_dense_capacity_short_reports_totals(engine):
     assert code == 17
     assert gd.total == acc.sum() == off[-1] > 0
     assert gd.total_values == (acc * np.diff(y_off)).sum() == voff[-1]
+
+
+def test_mixed_dense_device_arrays_match_host(engine):
+    """The mixed dense output with every array on the device equals the
+    host-memory call's."""
+    import torch
+    r = _chains([3, 16, 33, 64], seed=38, t_end=0.2)
+    rob = W.robertson(n=40, seed=39)
+    rob.t_end = np.full(rob.n, 5.0)
+    hu, hr = engine.bdf_solve_mixed(rob, r, dense=True)
+    dev = torch.device("cuda")
+    td = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    dr = W.RaggedBatch(r.name, r.rhs, td(r.y_off), td(r.p_off), td(r.y0), td(r.params), td(r.t0), td(r.t_end),
+                       r.tol, r.dt_min, r.dt_max, r.seed)
+    du = W.Batch(rob.name, rob.rhs, td(rob.y0), td(rob.params), td(rob.t0), td(rob.t_end), rob.tol, rob.dt_min,
+                 rob.dt_max, rob.seed)
+    us, rs = engine.bdf_solve_mixed(du, dr, dense=True)
+    for a, b in ((rs.traj_off, hr.traj_off), (rs.traj_voff, hr.traj_voff), (rs.traj_t, hr.traj_t),
+                 (rs.traj_y, hr.traj_y), (us.traj_off, hu.traj_off), (us.traj_t, hu.traj_t),
+                 (us.traj_y, hu.traj_y)):
+        np.testing.assert_array_equal(a.cpu().numpy(), b)
