@@ -69,6 +69,8 @@ class RkOptions(ctypes.Structure):
         ("blocks_per_sm", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
         ("schedule", ctypes.c_int32),
+        ("systems_per_warp", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -140,9 +140,9 @@ struct bacon_ctx {
   };
   std::unordered_map<uint64_t, Graph> graphs;
   // Autotuned launch per (kernel, batch size): kernel variant, threads per
-  // block, persistent CTAs per SM.
+  // block, persistent CTAs per SM, systems per warp (0: 32).
   struct Tuned {
-    int variant, block, bps;
+    int variant, block, bps, lanes;
   };
   std::unordered_map<uint64_t, Tuned> tuned;
   int force_variant = -1;  // set by the autotuner while it times a variant
@@ -720,16 +720,21 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   // and batch size (bacon_rk_autotune), else the occupancy model.
   int block = opt->block > 0 ? opt->block : 0;
   int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 0;
+  if (opt->systems_per_warp < 0 || opt->systems_per_warp > 32)
+    return fail(BACON_INVALID_ARGUMENT, "systems_per_warp must be 0..32");
+  int lanes = opt->systems_per_warp == 32 ? 0 : opt->systems_per_warp;
   const uint64_t tkey = tune_key(key, p->n);
   int variant = c->force_variant;
-  if (block == 0 && bps == 0 && variant < 0) {
+  if (block == 0 && bps == 0 && variant < 0 && lanes == 0) {
     auto it = c->tuned.find(tkey);
     if (it != c->tuned.end()) {
       variant = it->second.variant;
       block = it->second.block;
       bps = it->second.bps;
+      lanes = it->second.lanes;
     }
   }
+  a.lanes = lanes;
   if (variant > 0) {
     const void* vfn = nullptr;
     for (const auto& e : c->kernels)
@@ -738,7 +743,9 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
     fn = vfn;
   }
   const bool ff = opt->precision == BACON_FP32_COMP;
-  if (block == 0) block = bacon::default_block(p->n, c->num_sms, ff ? 256 : 128);
+  // systems per warp below 32: one-warp blocks, as many as the batch needs
+  const int spw = lanes > 0 ? lanes : 32;
+  if (block == 0) block = lanes > 0 ? 32 : bacon::default_block(p->n, c->num_sms, ff ? 256 : 128);
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
   int max_bps = 0;
   BACON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0));
@@ -746,7 +753,8 @@ extern "C" int bacon_rk_solve(bacon_ctx* c, const bacon_problem* p, const bacon_
   if (bps == 0) bps = model_blocks_per_sm(p->n, c->num_sms, block, max_bps, ff ? 768 : 256);
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(c->num_sms) * bps;
-  const long long need = (p->n + block - 1) / block;
+  const long long per_block = static_cast<long long>(block / 32) * spw;  // systems a block holds at a time
+  const long long need = (p->n + per_block - 1) / per_block;
   if (grid > need) grid = need;
 
   void* args[] = {&a};
@@ -823,6 +831,7 @@ static_assert(sizeof(bacon_rk_kernel_args) == sizeof(bacon::RkArgs), "kernel arg
 static_assert(offsetof(bacon_rk_kernel_args, traj_off) == offsetof(bacon::RkArgs, traj_off), "layout");
 static_assert(offsetof(bacon_rk_kernel_args, order) == offsetof(bacon::RkArgs, order), "layout");
 static_assert(offsetof(bacon_rk_kernel_args, ckpt_slots) == offsetof(bacon::RkArgs, ckpt_slots), "layout");
+static_assert(offsetof(bacon_rk_kernel_args, lanes) == offsetof(bacon::RkArgs, lanes), "layout");
 
 extern "C" int bacon_rk_solve_user(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                                    bacon_rk_result* r, bacon_rk_launch_fn launch, void* user) {
@@ -1821,11 +1830,36 @@ extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const 
       }
     }
   }
-  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{bv, bb, bs};
+  // Systems per warp below 32, for a batch too small to give every SM four
+  // warps of 32 (default kernel, one-warp blocks): less divergence within a
+  // warp where the FP64 pipe has room for more warps.
+  int bl = 0;
+  if (p->n <= static_cast<int64_t>(c->num_sms) * 32 * 4) {
+    c->force_variant = 0;
+    for (int lanes : {16, 8}) {
+      o.block = 32;
+      o.blocks_per_sm = 0;
+      o.systems_per_warp = lanes;
+      rc = bacon_rk_solve(c, p, &o, r);
+      if (rc == BACON_CUDA_ERROR || rc == BACON_INVALID_ARGUMENT || rc == BACON_UNSUPPORTED) return rc;
+      double ms = 0.0;
+      if (bacon_ctx_last_kernel_ms(c, &ms) != BACON_OK) return BACON_CUDA_ERROR;
+      ++count;
+      if (ms < best_ms) {
+        best_ms = ms;
+        bv = 0;
+        bb = 32;
+        bs = 0;  // as many one-warp blocks as the batch needs, up to the occupancy
+        bl = lanes;
+      }
+    }
+    o.systems_per_warp = 0;
+  }
+  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{bv, bb, bs, bl};
   if (out) {
     out->variant = bv;
     out->max_registers = bacon::variant_max_registers(bv);
-    out->systems_per_warp = 32;
+    out->systems_per_warp = bl > 0 ? bl : 32;
     out->block = bb;
     out->blocks_per_sm = bs;
     out->candidates = count;
@@ -1838,15 +1872,18 @@ extern "C" int bacon_rk_autotune_ex(bacon_ctx* c, const bacon_problem* p, const 
 extern "C" int bacon_rk_set_tuned(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* opt,
                                   const bacon_tune_result* t) {
   if (!c || !opt || !p || !t) return fail(BACON_INVALID_ARGUMENT, "NULL argument");
-  if (t->block % 32 != 0 || t->block < 32 || t->block > 256 || t->blocks_per_sm < 1)
-    return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32 in 32..256, blocks_per_sm >= 1");
+  if (t->block % 32 != 0 || t->block < 32 || t->block > 256 || t->blocks_per_sm < 0)
+    return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32 in 32..256, blocks_per_sm >= 0");
   const int layout = (opt->method == BACON_RK23 && opt->layout == BACON_LAYOUT_FEHLBERG) ? 1 : opt->layout;
   const bacon::RkKey key{opt->method, layout, opt->precision, p->rhs, p->dim};
   bool found = false;
   for (const auto& e : c->kernels)
     if (e.key == key && e.variant == t->variant) found = true;
   if (!found) return fail(BACON_UNSUPPORTED, "no such kernel variant for this (method, layout, precision, rhs, dim)");
-  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{t->variant, t->block, t->blocks_per_sm};
+  if (t->systems_per_warp < 0 || t->systems_per_warp > 32)
+    return fail(BACON_INVALID_ARGUMENT, "systems_per_warp must be 0..32");
+  const int lanes = t->systems_per_warp == 32 ? 0 : t->systems_per_warp;
+  c->tuned[tune_key(key, p->n)] = bacon_ctx::Tuned{t->variant, t->block, t->blocks_per_sm, lanes};
   return BACON_OK;
 }
 

@@ -174,7 +174,11 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
     a.order = oa.order;
   }
 
-  const int block = opt->block > 0 ? opt->block : bacon::default_block(p->n, num_sms, 128);
+  if (opt->systems_per_warp < 0 || opt->systems_per_warp > 32) return BACON_INVALID_ARGUMENT;
+  a.lanes = opt->systems_per_warp == 32 ? 0 : opt->systems_per_warp;
+  const int spw = a.lanes > 0 ? a.lanes : 32;
+  const int block =
+      opt->block > 0 ? opt->block : (a.lanes > 0 ? 32 : bacon::default_block(p->n, num_sms, 128));
   if (block % 32 != 0 || block > 256) return BACON_INVALID_ARGUMENT;
   int max_bps = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, fn, block, 0) != cudaSuccess || max_bps < 1)
@@ -182,7 +186,8 @@ extern "C" int bacon_rk_solve_noalloc(const bacon_problem* p, const bacon_rk_opt
   int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : max_bps;
   if (bps > max_bps) bps = max_bps;
   long long grid = static_cast<long long>(num_sms) * bps;
-  const long long need = (p->n + block - 1) / block;
+  const long long per_block = static_cast<long long>(block / 32) * spw;  // systems a block holds at a time
+  const long long need = (p->n + per_block - 1) / per_block;
   if (grid > need) grid = need;
 
   // The array keeps the previous call's contents: reset the counters.

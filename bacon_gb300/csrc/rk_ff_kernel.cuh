@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_ff_kernel(const
   double t = 0.0, end = 0.0, dt = 0.0;
   int32_t acc = 0, rej = 0;
   int64_t attempts = 0, idx = 0;
-  bool have = false, exhausted = false;
+  bool have = false, exhausted = a.lanes > 0 && static_cast<int>(lane) >= a.lanes;  // as rk_persistent_kernel
 
   for (;;) {
     const bool need = !have && !exhausted;

@@ -60,6 +60,7 @@ struct RkArgs {
   int32_t ckpt_every;
   int32_t max_steps;
   int32_t ckpt_slots;
+  int32_t lanes;  // systems per warp: lanes 0..lanes-1 take systems (0: all 32)
 };
 
 template <int I, int N, class F>
@@ -114,7 +115,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) rk_persistent_kernel(const Rk
   double t = 0.0, end = 0.0, dt = 0.0;
   int32_t acc = 0, rej = 0;
   int64_t attempts = 0, idx = 0;
-  bool have = false, exhausted = false;
+  // lanes beyond a.lanes never take a system; they stay in the loop's
+  // warp-wide votes (full masks) and idle
+  bool have = false, exhausted = a.lanes > 0 && static_cast<int>(lane) >= a.lanes;
 
   for (;;) {
     // ---- pull new systems for idle lanes (one atomic per warp) ----

@@ -148,13 +148,14 @@ def make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim=False,
 
 
 def rk_options(method=RK45, layout=FEHLBERG, precision=FP64_EXACT, memory=MEM_HOST, max_attempts=0,
-               block=0, blocks_per_sm=0, use_graph=True, schedule=0):
+               block=0, blocks_per_sm=0, use_graph=True, schedule=0, systems_per_warp=0):
     o = _capi.RkOptions()
     o.method, o.layout, o.precision, o.memory = method, layout, precision, memory
     o.max_attempts = int(max_attempts)
     o.block, o.blocks_per_sm = int(block), int(blocks_per_sm)
     o.use_graph = int(bool(use_graph))
     o.schedule = int(schedule)
+    o.systems_per_warp = int(systems_per_warp)
     return o
 
 
@@ -231,7 +232,8 @@ def _dense_call(fn, handle, prob, opts, out, device, dim, n, capacity):
 def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, layout=FEHLBERG,
              precision=FP64_EXACT, max_attempts=0, traj_cap=0, ctx: Context | None = None,
              plain=False, block=0, blocks_per_sm=0, use_graph=True, dyn_dim=False, out=None,
-             raise_on_error=False, schedule=0, shared=None, dense=False, dense_capacity=None) -> Solution:
+             raise_on_error=False, schedule=0, shared=None, dense=False, dense_capacity=None,
+             systems_per_warp=0) -> Solution:
     """Batched RK45/RK23 solve.  Inputs are all numpy (host) or all CUDA tensors.
     ``shared``: the dim x dim matrix of BACON_RHS_LINEAR (row-major).
     ``dense``: every yielded item of every system, packed (bacon_rk_solve_dense):
@@ -251,7 +253,7 @@ def rk_solve(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45, la
     dim, n = int(y0.shape[0]), int(y0.shape[1])
     prob = make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, rhs, dyn_dim, shared)
     opts = rk_options(method, layout, precision, MEM_DEVICE if device else MEM_HOST, max_attempts,
-                      block, blocks_per_sm, use_graph, schedule)
+                      block, blocks_per_sm, use_graph, schedule, systems_per_warp)
     if out is None:
         out = alloc_outputs(dim, n, device, traj_cap)
     lib = _capi.load()
@@ -353,9 +355,9 @@ def rk_autotune(y0, params, t0, t_end, *, rhs, tol, dt_min, dt_max, method=RK45,
 
 
 def rk_set_tuned(y0, *, rhs, variant, block, blocks_per_sm, method=RK45, layout=FEHLBERG, precision=FP64_EXACT,
-                 ctx: Context | None = None):
-    """Pin the kernel variant and launch shape the context uses for this
-    kernel and batch size (bacon_rk_set_tuned)."""
+                 ctx: Context | None = None, systems_per_warp=32):
+    """Pin the kernel variant, launch shape and systems per warp the
+    context uses for this kernel and batch size (bacon_rk_set_tuned)."""
     ctx = ctx or default_context()
     dim, n = int(y0.shape[0]), int(y0.shape[1])
     prob = _capi.Problem()
@@ -363,6 +365,7 @@ def rk_set_tuned(y0, *, rhs, variant, block, blocks_per_sm, method=RK45, layout=
     opts = rk_options(method, layout, precision)
     t = _capi.TuneResult()
     t.variant, t.block, t.blocks_per_sm = int(variant), int(block), int(blocks_per_sm)
+    t.systems_per_warp = int(systems_per_warp)
     check(_capi.load().bacon_rk_set_tuned(ctx.handle, ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(t)))
 
 

@@ -50,6 +50,8 @@ pub struct bacon_rk_options {
     pub blocks_per_sm: i32,
     pub use_graph: i32,
     pub schedule: i32,
+    pub systems_per_warp: i32,
+    pub reserved: i32,
 }
 
 #[repr(C)]
@@ -150,6 +152,7 @@ pub struct bacon_rk_kernel_args {
     pub ckpt_every: i32,
     pub max_steps: i32,
     pub ckpt_slots: i32,
+    pub lanes: i32,
 }
 
 #[repr(C)]

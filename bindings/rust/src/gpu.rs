@@ -548,6 +548,8 @@ impl<const METHOD: i32> GpuRungeKutta<METHOD> {
             blocks_per_sm: 0,
             use_graph: 1,
             schedule: 0,
+            systems_per_warp: 0,
+            reserved: 0,
         }
     }
 

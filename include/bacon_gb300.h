@@ -172,6 +172,11 @@ typedef struct {
    * systems have per-system start or end times, index order otherwise;
    * 1 = index order; 2 = longest span first. */
   int32_t schedule;
+  /* Systems a warp integrates at a time, 1..32 (the others of its lanes
+   * idle); 0 = 32, or the autotuned count.  Fewer than 32 pays only for a
+   * batch too small to fill the GPU, by cutting divergence within warps. */
+  int32_t systems_per_warp;
+  int32_t reserved;
 } bacon_rk_options;
 
 /* Outputs, same memory kind as the inputs.  (t_final, y_final) is the last
@@ -215,14 +220,15 @@ int bacon_rk_autotune(bacon_ctx* ctx, const bacon_problem* problem,
                       int32_t* best_block, int32_t* best_blocks_per_sm);
 
 /* What the autotuner chose for a batch, and what it measured.  The
- * persistent kernels keep one system per lane (32 systems per warp): the
- * FP64 pipe charges a warp instruction the same time however few lanes are
- * active, so splitting a system across lanes multiplies its FP64 time.  The
- * choices are the register budget (kernel variant) and the launch shape. */
+ * persistent kernels keep a system on one lane: the FP64 pipe charges a warp
+ * instruction the same time however few lanes are active, so splitting a
+ * system across lanes multiplies its FP64 time.  The choices are the
+ * register budget (kernel variant), the launch shape and, for a batch too
+ * small to fill the GPU, the systems per warp (32, 16 or 8). */
 typedef struct {
   int32_t variant;          /* 0: default kernel; 1, 2: register-capped variants */
   int32_t max_registers;    /* the variant's budget per thread, 0 = the compiler's */
-  int32_t systems_per_warp; /* 32 */
+  int32_t systems_per_warp; /* lanes per warp that take systems */
   int32_t block;            /* threads per block */
   int32_t blocks_per_sm;    /* persistent CTAs per SM */
   int32_t candidates;       /* (variant, shape) pairs timed */
@@ -289,6 +295,7 @@ typedef struct {
   int32_t ckpt_every;
   int32_t max_steps;
   int32_t ckpt_slots;
+  int32_t lanes;
 } bacon_rk_kernel_args;
 
 /* Launches the caller's kernel for (method, layout, precision) with `grid`

@@ -27,8 +27,9 @@ def test_autotune_register_budget_variants_identical(engine):
     before = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
     t = engine.rk_autotune(b.y0, b.params, b.t0, b.t_end, details=True, **kw)
     # shapes that the occupancy caps onto one already timed are timed once,
-    # and the shape reported is the one launched
-    assert 8 <= t["candidates"] <= 8 + 2 * 4
+    # and the shape reported is the one launched; a batch this small also
+    # gets 16 and 8 systems per warp
+    assert 8 <= t["candidates"] <= 8 + 2 * 4 + 2
     if t["max_registers"]:
         assert t["block"] * t["blocks_per_sm"] * t["max_registers"] <= 65536
     assert t["variant"] in (0, 1, 2) and t["max_registers"] in (0, 80, 64)
@@ -46,3 +47,37 @@ def test_autotune_register_budget_variants_identical(engine):
             np.testing.assert_array_equal(out.y, ref.y)
             np.testing.assert_array_equal(out.rejected, ref.rejected)
         ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_systems_per_warp_keeps_results(engine, precision):
+    """Fewer systems per warp (the other lanes idle) changes which lanes run
+    which systems, never a system's arithmetic: bit-identical results."""
+    b = W.van_der_pol(n=4096, seed=91)
+    kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2, precision=precision)
+    ref = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, **kw)
+    for spw in (16, 8, 1):
+        out = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, systems_per_warp=spw, **kw)
+        np.testing.assert_array_equal(out.y, ref.y)
+        np.testing.assert_array_equal(out.accepted, ref.accepted)
+        np.testing.assert_array_equal(out.rejected, ref.rejected)
+        np.testing.assert_array_equal(out.status, ref.status)
+
+
+def test_autotune_small_batch_tries_systems_per_warp(engine):
+    """On a batch too small to fill the GPU the tuner also times 16 and 8
+    systems per warp; whatever it caches keeps the results."""
+    b = W.van_der_pol(n=4096, seed=92)
+    kw = dict(rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
+    ctx = engine.Context(0)
+    ref = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, ctx=ctx, **kw)
+    t = engine.rk_autotune(b.y0, b.params, b.t0, b.t_end, details=True, ctx=ctx, **kw)
+    assert t["systems_per_warp"] in (8, 16, 32)
+    assert t["candidates"] >= 8 + 2
+    out = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, ctx=ctx, **kw)
+    np.testing.assert_array_equal(out.y, ref.y)
+    np.testing.assert_array_equal(out.accepted, ref.accepted)
+    engine.rk_set_tuned(b.y0, rhs=b.rhs, variant=0, block=32, blocks_per_sm=0, systems_per_warp=8, ctx=ctx)
+    out = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, ctx=ctx, **kw)
+    np.testing.assert_array_equal(out.y, ref.y)
+    ctx.close()

@@ -24,11 +24,11 @@ def _device(a):
     return torch.from_numpy(np.ascontiguousarray(a)).to(torch.device("cuda"))
 
 
-def _noalloc(E, L, prob, layout, n, dim):
+def _noalloc(E, L, prob, layout, n, dim, systems_per_warp=0):
     import torch
     out = E.alloc_outputs(dim, n, device=True)
     res = E.make_result(out)
-    opts = E.rk_options(layout=layout, memory=E.MEM_DEVICE)
+    opts = E.rk_options(layout=layout, memory=E.MEM_DEVICE, systems_per_warp=systems_per_warp)
     torch.cuda.synchronize()
     code = L.bacon_rk_solve_noalloc(ctypes.byref(prob), ctypes.byref(opts), ctypes.byref(res), None)
     return code, out
@@ -129,3 +129,17 @@ def test_noalloc_zero_size_warm_up_then_no_device_memory_change(engine):
     for out in outs:
         _assert_same(out, ref)
 
+
+
+def test_noalloc_systems_per_warp(engine):
+    """Eight systems per warp through the allocation-free entry point: the
+    same results as the regular entry point at 32."""
+    from bacon_gb300 import _capi
+    L = _capi.load()
+    b = W.van_der_pol(n=4096, seed=93)
+    y0, prm, t0, te = (_device(x) for x in (b.y0, b.params, b.t0, b.t_end))
+    ref = engine.rk_solve(y0, prm, t0, te, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, layout=2)
+    prob = engine.make_problem(y0, prm, t0, te, b.tol, b.dt_min, b.dt_max, b.rhs)
+    code, out = _noalloc(engine, L, prob, 2, b.n, 2, systems_per_warp=8)
+    assert code == 0
+    _assert_same(out, ref)
