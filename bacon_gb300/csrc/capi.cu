@@ -883,11 +883,16 @@ extern "C" int bacon_rk_solve_user(bacon_ctx* c, const bacon_problem* p, const b
                           c->ord_scratch.as<bacon::OrderScratch>(), c->ord.as<uint32_t>()};
     a.order = oa.order;
   }
-  const int block = opt->block > 0 ? opt->block : 128;
+  if (opt->systems_per_warp < 0 || opt->systems_per_warp > 32)
+    return fail(BACON_INVALID_ARGUMENT, "systems_per_warp must be 0..32");
+  a.lanes = opt->systems_per_warp == 32 ? 0 : opt->systems_per_warp;
+  const int spw = a.lanes > 0 ? a.lanes : 32;
+  const int block = opt->block > 0 ? opt->block : (a.lanes > 0 ? 32 : bacon::default_block(p->n, c->num_sms, 128));
   if (block % 32 != 0 || block > 256) return fail(BACON_INVALID_ARGUMENT, "block must be a multiple of 32, <= 256");
-  const int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : 2;
+  const int bps = opt->blocks_per_sm > 0 ? opt->blocks_per_sm : (a.lanes > 0 ? 8 : 2);
   long long grid = static_cast<long long>(c->num_sms) * bps;
-  const long long need = (p->n + block - 1) / block;
+  const long long per_block = static_cast<long long>(block / 32) * spw;  // systems a block holds at a time
+  const long long need = (p->n + per_block - 1) / per_block;
   if (grid > need) grid = need;
   if (host && (rc = enqueue_h2d(c, p, o)) != BACON_OK) return rc;
   if (lpt) BACON_CUDA(bacon::enqueue_lpt_order(oa, c->num_sms, c->stream));

@@ -39,10 +39,11 @@ def user_lib():
     return ctypes.CDLL(out)
 
 
-def _solve_user(engine, lib, launcher, y0, params, t0, t_end, tol, dt_min, dt_max, precision=0, layout=2):
+def _solve_user(engine, lib, launcher, y0, params, t0, t_end, tol, dt_min, dt_max, precision=0, layout=2,
+                systems_per_warp=0):
     from bacon_gb300 import _capi
     prob = engine.make_problem(y0, params, t0, t_end, tol, dt_min, dt_max, 11)  # BACON_RHS_USER
-    opts = engine.rk_options(layout=layout, precision=precision)
+    opts = engine.rk_options(layout=layout, precision=precision, systems_per_warp=systems_per_warp)
     out = engine.alloc_outputs(y0.shape[0], y0.shape[1], device=False)
     res = engine.make_result(out)
     fn = ctypes.cast(getattr(lib, launcher), ctypes.c_void_p)
@@ -59,12 +60,13 @@ def test_user_van_der_pol_is_the_registry_bit_for_bit(engine, user_lib):
         if precision == 1:
             ref = engine.rk_solve(b.y0, b.params, 0.0, 10.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min,
                                   dt_max=b.dt_max, layout=2, precision=1)
-        code, out = _solve_user(engine, user_lib, "user_vdp_launch", b.y0, b.params, 0.0, 10.0, b.tol, b.dt_min,
-                                b.dt_max, precision=precision)
-        assert code == ref.code == 0
-        np.testing.assert_array_equal(out["y"], ref.y)
-        np.testing.assert_array_equal(out["accepted"], ref.accepted)
-        np.testing.assert_array_equal(out["rejected"], ref.rejected)
+        for spw in (0, 8):
+            code, out = _solve_user(engine, user_lib, "user_vdp_launch", b.y0, b.params, 0.0, 10.0, b.tol,
+                                    b.dt_min, b.dt_max, precision=precision, systems_per_warp=spw)
+            assert code == ref.code == 0
+            np.testing.assert_array_equal(out["y"], ref.y)
+            np.testing.assert_array_equal(out["accepted"], ref.accepted)
+            np.testing.assert_array_equal(out["rejected"], ref.rejected)
 
 
 def test_user_duffing_vs_dop853(engine, user_lib):
