@@ -6,7 +6,7 @@
     python -m bacon_gb300.cases linear --n 8192 [--precision tc_split]
     python -m bacon_gb300.cases adjoint --n 16384
     python -m bacon_gb300.cases vdp --n 4096
-    python -m bacon_gb300.cases adams --n 4096
+    python -m bacon_gb300.cases adams --n 4096 [--t-end 1]
 
 Each case generates the workload's seeded batch at the given size (the
 workload generators in workloads.py), solves it `--repeat` times through the
@@ -48,7 +48,7 @@ def _counts(status):
     return {int(k): int((s == k).sum()) for k in np.unique(s)}
 
 
-def run(case: str, n: int, precision: str, repeat: int, tuned: tuple | None = None) -> dict:
+def run(case: str, n: int, precision: str, repeat: int, tuned: tuple | None = None, t_end: float = 10.0) -> dict:
     import torch
     ctx = E.Context(0)
     prec = PRECISION[precision]
@@ -74,7 +74,7 @@ def run(case: str, n: int, precision: str, repeat: int, tuned: tuple | None = No
         elif case == "adams":
             b = W.van_der_pol(n=n)
             y0, p = _dev(torch, b.y0, b.params)
-            s = E.adams_solve(y0, p, 0.0, 10.0, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, order=5,
+            s = E.adams_solve(y0, p, 0.0, t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max, order=5,
                               ctx=ctx)
             out["status"] = _counts(s.status)
         elif case == "adjoint":
@@ -111,11 +111,12 @@ def main() -> None:
     ap.add_argument("--precision", default="fp64_exact", choices=sorted(PRECISION))
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--tuned", default=None, help="VARIANT,BLOCK,CTAS_PER_SM for lorenz / vdp")
+    ap.add_argument("--t-end", type=float, default=10.0, help="end time of the adams case (the workload's is 10)")
     a = ap.parse_args()
     tuned = tuple(int(x) for x in a.tuned.split(",")) if a.tuned else None
     if tuned is not None and len(tuned) != 3:
         raise SystemExit("--tuned wants VARIANT,BLOCK,CTAS_PER_SM")
-    print(json.dumps(run(a.case, a.n, a.precision, a.repeat, tuned)))
+    print(json.dumps(run(a.case, a.n, a.precision, a.repeat, tuned, a.t_end)))
 
 
 if __name__ == "__main__":
