@@ -261,7 +261,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
   const int lane = tid % 32;
   const int64_t n = a.st.n;
   const int64_t ntx = (n + kTcN - 1) / kTcN;
-  const int64_t ntiles = ntx * (D / kTcM);
+  // The row tiles of one system tile are consecutive tiles, so the CTAs that
+  // take them run at about the same time and the second read of the system
+  // tile's slices hits L2 (at 65,536 systems the slices of all tiles, 168 MB,
+  // exceed it).
+  constexpr int kRowTiles = D / kTcM;
+  const int64_t ntiles = ntx * kRowTiles;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_sh)),
@@ -297,8 +302,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
     bool inflight[2] = {false, false};  // copies issued, their arrival not yet waited for
     bool ok = true, first = true;
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int r0 = static_cast<int>(tile / ntx) * kTcM;
-      const int64_t s0 = (tile % ntx) * kTcN;
+      const int r0 = static_cast<int>(tile % kRowTiles) * kTcM;
+      const int64_t s0 = (tile / kRowTiles) * kTcN;
       const int64_t sa0 = s0 + lane, sa1 = s0 + 32 + lane;
       const bool live = (sa0 < n && a.st.status[sa0] == kLinRunning) || (sa1 < n && a.st.status[sa1] == kLinRunning);
       if (!__any_sync(0xffffffffu, live)) continue;
@@ -390,8 +395,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) lin_tc_stage_kernel(const TcArg
     const int cbase = (warp / 4) * 32;
     uint32_t tphase = 0u;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-      const int r0 = static_cast<int>(tile / ntx) * kTcM;
-      const int64_t s0 = (tile % ntx) * kTcN;
+      const int r0 = static_cast<int>(tile % kRowTiles) * kTcM;
+      const int64_t s0 = (tile / kRowTiles) * kTcN;
       tc_epi_sync();  // the previous tile's readers of tile_* are done
       if (tid < kTcN) {
         // the epilogue's per-system data, read once per tile
