@@ -584,8 +584,10 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
   // persistent stage GEMM: one CTA per SM over (systems / 64) x (D / 128) tiles
   const long long tc_tiles = ((n + bacon::kTcN - 1) / bacon::kTcN) * (D / bacon::kTcM);
   const dim3 tg(static_cast<unsigned>(tc_tiles < c->num_sms ? tc_tiles : c->num_sms));
-  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
-  while (*h_live > 0) {
+  // One round: the S products (or stage GEMMs), the live-counter reset, the
+  // control kernel and the copies the host reads.  It is captured once as a
+  // CUDA graph and relaunched until no system runs, one launch per round.
+  auto enqueue_round = [&]() -> int {
     for (int s = 0; s < k.stages; ++s) {
       if (tc) {
         // v_{s+1} = A v_s into K[s], v_0 = y
@@ -597,7 +599,6 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
         BACON_CUDA(cudaLaunchKernel(s + 1 == k.stages ? tk.gemm_last : tk.gemm, tg,
                                     dim3(static_cast<unsigned>(tk.gemm_threads)), gargs,
                                     static_cast<size_t>(tk.smem_bytes), c->stream));
-        c->launches += 1;
       } else {
         BACON_CUDA(cudaLaunchKernel(k.stage[s], sg, dim3(256), sargs, 0, c->stream));
       }
@@ -608,8 +609,33 @@ int linear_solve(bacon_ctx* c, const bacon_problem* p, const bacon_rk_options* o
     if (tc)  // a tensor-core stage that gave up a bounded wait ends the solve
       BACON_CUDA(cudaMemcpyAsync(c->h_ctl + 3, c->d_ctl + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  c->stream));
+    return BACON_OK;
+  };
+  struct RoundGraph {
+    cudaGraphExec_t exec = nullptr;
+    ~RoundGraph() {
+      if (exec) cudaGraphExecDestroy(exec);
+    }
+  } round;
+  BACON_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const int erc = enqueue_round();
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+  if (erc != BACON_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return erc;
+  }
+  if (ce != cudaSuccess) return fail(BACON_CUDA_ERROR, std::string("round graph capture: ") + cudaGetErrorString(ce));
+  const cudaError_t ie = cudaGraphInstantiate(&round.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess)
+    return fail(BACON_CUDA_ERROR, std::string("round graph instantiate: ") + cudaGetErrorString(ie));
+  const int per_round = (tc ? 2 * k.stages : k.stages) + 1;  // kernels in one round
+  BACON_CUDA(cudaEventRecord(c->ev0, c->stream));
+  while (*h_live > 0) {
+    BACON_CUDA(cudaGraphLaunch(round.exec, c->stream));
     BACON_CUDA(cudaStreamSynchronize(c->stream));
-    c->launches += k.stages + 1;
+    c->launches += per_round;
     if (tc && c->h_ctl[3] != 0) return fail(BACON_CUDA_ERROR, "tensor-core stage: a bounded mbarrier wait gave up");
   }
   BACON_CUDA(cudaEventRecord(c->ev1, c->stream));
