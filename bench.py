@@ -647,6 +647,7 @@ def main():
         lref = A.reference_final_states(lsb)
         extras["final_state_error_vs_rtol1e-12"] = {
             "fp64_exact": A.final_state_error(out["y"].cpu().numpy()[:, short], lref),
+            "fp64_fma": A.final_state_error(fout["y"].cpu().numpy()[:, short], lref),
             "fp32_comp": A.final_state_error(cout["y"].cpu().numpy()[:, short], lref),
             "sample": f"{short.size} Lorenz systems with T <= 5 (chaotic: error grows with T)"}
 
@@ -807,6 +808,7 @@ def compact_summary(line):
         "adams5_cpu_16core_solves_s": r3(g("adams5_van_der_pol_4096", "cpu_baseline", "value")),
         "final_state_rel_max_vs_rtol1e-12": {
             "lorenz_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp64_exact", "rel_max")),
+            "lorenz_fma_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp64_fma", "rel_max")),
             "lorenz_fp32comp_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp32_comp", "rel_max")),
             "vdp": r3(g("van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
             "adams5_vdp": r3(g("adams5_van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
