@@ -81,3 +81,11 @@ def test_autotune_small_batch_tries_systems_per_warp(engine):
     out = engine.rk_solve(b.y0, b.params, b.t0, b.t_end, ctx=ctx, **kw)
     np.testing.assert_array_equal(out.y, ref.y)
     ctx.close()
+
+
+def test_systems_per_warp_out_of_range_rejected(engine):
+    b = W.van_der_pol(n=64, seed=94)
+    with pytest.raises(engine.IVPError) as err:
+        engine.rk_solve(b.y0, b.params, b.t0, b.t_end, rhs=b.rhs, tol=b.tol, dt_min=b.dt_min, dt_max=b.dt_max,
+                        layout=2, systems_per_warp=33, raise_on_error=True)
+    assert "systems_per_warp" in str(err.value)

@@ -211,3 +211,17 @@ def test_mixed_dense_device_arrays_match_host(engine):
                  (rs.traj_y, hr.traj_y), (us.traj_off, hu.traj_off), (us.traj_t, hu.traj_t),
                  (us.traj_y, hu.traj_y)):
         np.testing.assert_array_equal(a.cpu().numpy(), b)
+
+
+def test_mixed_dense_uniform_part_only(engine, oracle):
+    """The mixed dense call with no ragged part records the uniform part's
+    items exactly as bacon_bdf_solve_dense does."""
+    rob = W.robertson(n=24, seed=44)
+    rob.t_end = np.full(rob.n, 3.0)
+    us, rs = engine.bdf_solve_mixed(rob, None, dense=True)
+    assert rs is None and us.code == 0
+    ref = engine.bdf_solve(rob.y0, rob.params, 0.0, 3.0, rhs=rob.rhs, tol=rob.tol, dt_min=rob.dt_min,
+                           dt_max=rob.dt_max, dense=True)
+    np.testing.assert_array_equal(np.asarray(us.traj_off), np.asarray(ref.traj_off))
+    np.testing.assert_array_equal(us.traj_t, ref.traj_t)
+    np.testing.assert_array_equal(us.traj_y, ref.traj_y)
