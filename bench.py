@@ -331,13 +331,24 @@ def other_workloads(E, W, ctx, dev, torch, ext, flush, fp64_peak_tflops, stiff_n
     vacc = s.accepted.cpu().numpy().astype(np.int64)
     vrej = s.rejected.cpu().numpy().astype(np.int64)
     vfl = R.rk_flops(0, vb.rhs, 2, int(vacc.sum() + vrej.sum()), int(vacc.sum()))
+    # the same batch in the FP32-stage mode (float-float stages, FP64 control)
+    E.rk_solve(vy, vp, 0.0, 10.0, precision=E.FP32_COMP, **kw)
+    fkms = []
+    for _ in range(3):
+        fs = E.rk_solve(vy, vp, 0.0, 10.0, precision=E.FP32_COMP, **kw)
+        fkms.append(ctx.last_kernel_ms())
+    fms_v = statistics.median(fkms)
     out["van_der_pol_4096"] = {
         "value": vb.n / (ms * 1e-3), "unit": "solves/s", "kernel_ms": ms,
         "statuses_ok": bool((s.status == 0).all().item()),
         "final_state_error_vs_rtol1e-12": ok_error(s.y.cpu().numpy(), vref, s.status.cpu().numpy()),
         "roofline": {"bound": "fp64", "achieved": vfl / (ms * 1e-3) / 1e12, "peak": fp64_peak_tflops,
                      "unit": "TFLOP/s", "frac": vfl / (ms * 1e-3) / 1e12 / fp64_peak_tflops,
-                     "note": "4096 threads fill 32 of the 152 SMs"}}
+                     "note": "4096 systems as one-warp blocks on 128 of the 152 SMs: the launch lasts as long as "
+                             "its slowest system's chain of dependent FP64 operations"},
+        "fp32_comp": {"value": vb.n / (fms_v * 1e-3), "unit": "solves/s", "kernel_ms": fms_v,
+                      "statuses_ok": bool((fs.status == 0).all().item()),
+                      "final_state_error_vs_rtol1e-12": ok_error(fs.y.cpu().numpy(), vref, fs.status.cpu().numpy())}}
 
     # The same Van der Pol batch with Adams5 (the reference's predictor-
     # corrector, src/ivp/adams.rs): it restarts from an RK4 bootstrap after
@@ -803,7 +814,9 @@ def compact_summary(line):
                   "frac": r3(g("bdf6_stiff", "roofline", "frac"))},
         "linear_tc": {"solves_s": r3(g("linear_shared_A_256", "tensor_split", "value")),
                       "frac_bf16": r3(g("linear_shared_A_256", "tensor_split", "roofline", "frac"))},
-        "vdp_solves_s": r3(g("van_der_pol_4096", "value")), "adams5_solves_s": r3(g("adams5_van_der_pol_4096", "value")),
+        "vdp_solves_s": r3(g("van_der_pol_4096", "value")),
+        "vdp_fp32comp_solves_s": r3(g("van_der_pol_4096", "fp32_comp", "value")),
+        "adams5_solves_s": r3(g("adams5_van_der_pol_4096", "value")),
         "adams5_65536_solves_s": r3(g("adams5_van_der_pol_65536", "value")),
         "adams5_cpu_16core_solves_s": r3(g("adams5_van_der_pol_4096", "cpu_baseline", "value")),
         "final_state_rel_max_vs_rtol1e-12": {
@@ -811,6 +824,7 @@ def compact_summary(line):
             "lorenz_fma_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp64_fma", "rel_max")),
             "lorenz_fp32comp_T_le_5": r3(g("final_state_error_vs_rtol1e-12", "fp32_comp", "rel_max")),
             "vdp": r3(g("van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
+            "vdp_fp32comp": r3(g("van_der_pol_4096", "fp32_comp", "final_state_error_vs_rtol1e-12", "rel_max")),
             "adams5_vdp": r3(g("adams5_van_der_pol_4096", "final_state_error_vs_rtol1e-12", "rel_max")),
             "lv": r3(g("adjoint", "final_state_error_vs_rtol1e-12", "rel_max")),
             "robertson_abs": r3(g("bdf6_stiff", "final_state_error_vs_rtol1e-12", "robertson_vs_radau", "abs_max")),
