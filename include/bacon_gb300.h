@@ -99,10 +99,10 @@ typedef enum {
   BACON_FP64_EXACT = 0,
   BACON_FP64_FMA = 1,
   BACON_FP32_COMP = 2,
-  /* BACON_RHS_LINEAR only: the stage GEMM on tcgen05 tensor cores, bf16
-   * integer slices of A and Y (5 x 8 bits, Ozaki splitting) with FP32
-   * accumulation, exact on the three leading diagonals, combined in FP64;
-   * relative error of A*Y ~ 2^-39. */
+  /* BACON_RHS_LINEAR only: the products A^k y an attempt needs, as GEMMs on
+   * the tcgen05 tensor cores: bf16 integer slices of A and of the vectors
+   * (5 x 8 bits, Ozaki splitting) with FP32 accumulation, exact on the
+   * three leading diagonals, combined in FP64; relative error ~ 2^-39. */
   BACON_TC_SPLIT = 3
 } bacon_precision;
 
