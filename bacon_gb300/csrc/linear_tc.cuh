@@ -524,14 +524,11 @@ __device__ __forceinline__ void tc_load_run(const double* p, double (&v)[PER]) {
   }
 }
 
-// The system's exponent and the slices of its PER values from PER*lane (one
-// warp per system).
+// The slices of a system's PER values from PER*lane (one warp per system,
+// every lane of the warp calling it) and its exponent.
 template <int D>
-__device__ __forceinline__ void tc_slice_store(const double (&v)[D / 32], unsigned lane, int64_t sys,
-                                               __nv_bfloat16* sy, int32_t* ey) {
+__device__ __forceinline__ int tc_slice_values(const double (&v)[D / 32], __nv_bfloat16 (&qs)[D / 32][kTcSlices]) {
   constexpr int PER = D / 32;
-  static_assert(PER == 4 || PER == 8, "vector stores of 8 or 16 bytes");
-  using Vec = typename TcSliceVec<PER>::T;
   unsigned long long mx = 0ull;
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
@@ -544,34 +541,72 @@ __device__ __forceinline__ void tc_slice_store(const double (&v)[D / 32], unsign
     mx = other > mx ? other : mx;
   }
   const int e = tc_exponent_of(mx);
-  if (lane == 0) ey[sys] = e;
-  __nv_bfloat16 qs[PER][kTcSlices];
 #pragma unroll
   for (int i = 0; i < PER; ++i) tc_slices(v[i], e, qs[i]);
+  return e;
+}
+
+// Slices of the vectors x (per system contiguous, [n][D]) of the running
+// systems: y, or the product v_k = A^k y for the next one.  A block of eight
+// warps takes eight consecutive systems, one each.  In a chunk image those
+// eight systems' entries of one (chunk, slice) block are one contiguous run
+// of 8 x 32 values (512 B), so the warps assemble the runs in shared memory
+// and the block writes them with whole 16-byte stores across lines, instead
+// of every lane scattering 16 bytes into eight different 128-byte lines.
+// Systems that are not running (or past n) get zero slices: the GEMM's
+// epilogue skips their columns.
+template <int D>
+__global__ void __launch_bounds__(256) lin_tc_slice_vec_kernel(const TcArgs a, const double* x, __nv_bfloat16* sy,
+                                                               int32_t* ey) {
+  constexpr int PER = D / 32;
+  constexpr int kChunks = D / kTcKc;
+  constexpr int kRun = kTcKc * 8;  // values of one (chunk, slice) run of 8 systems
+  static_assert(PER == 4 || PER == 8, "vector stores of 8 or 16 bytes");
+  static_assert(kTcN % 8 == 0, "8-system groups within a tile");
+  using Vec = typename TcSliceVec<PER>::T;
+  __shared__ __align__(16) __nv_bfloat16 staged[kChunks * kTcSlices * kRun];
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = static_cast<int>(threadIdx.x >> 5);
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * 8;
+  const int64_t sys = first + w;
+  const bool run = sys < a.st.n && a.st.status[sys] == kLinRunning;  // the same for the whole warp
+  __nv_bfloat16 qs[PER][kTcSlices];
+  if (run) {
+    double v[PER];
+    tc_load_run<PER>(x + sys * D + PER * lane, v);
+    const int e = tc_slice_values<D>(v, qs);
+    if (lane == 0) ey[sys] = e;
+  } else {
 #pragma unroll
-  for (int s = 0; s < kTcSlices; ++s) {
+    for (int i = 0; i < PER; ++i)
+#pragma unroll
+      for (int q = 0; q < kTcSlices; ++q) qs[i][q] = __float2bfloat16_rz(0.0f);
+  }
+  // this lane's PER values are contiguous in the run: chunk c, at
+  // (kk / 8) * 64 + w * 8 + kk % 8 for its first K index kk in the chunk
+  const int k0 = PER * static_cast<int>(lane);
+  const int c = k0 / kTcKc, kk = k0 % kTcKc;
+  const int intra = (kk / 8) * 64 + w * 8 + (kk % 8);
+#pragma unroll
+  for (int q = 0; q < kTcSlices; ++q) {
     union {
       Vec vec;
       __nv_bfloat16 h[PER];
     } u;
 #pragma unroll
-    for (int i = 0; i < PER; ++i) u.h[i] = qs[i][s];
-    *reinterpret_cast<Vec*>(sy + tc_tile_index<D>(kTcN, sys, s, PER * static_cast<int>(lane))) = u.vec;
+    for (int i = 0; i < PER; ++i) u.h[i] = qs[i][q];
+    *reinterpret_cast<Vec*>(staged + (c * kTcSlices + q) * kRun + intra) = u.vec;
   }
-}
-
-// Slices of the vectors x (per system contiguous, [n][D]) of the running
-// systems: y, or the product v_k = A^k y for the next one.
-template <int D>
-__global__ void __launch_bounds__(256) lin_tc_slice_vec_kernel(const TcArgs a, const double* x, __nv_bfloat16* sy,
-                                                               int32_t* ey) {
-  constexpr int PER = D / 32;
-  const unsigned lane = threadIdx.x & 31u;
-  const int64_t sys = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
-  if (sys >= a.st.n || a.st.status[sys] != kLinRunning) return;
-  double v[PER];
-  tc_load_run<PER>(x + sys * D + PER * lane, v);
-  tc_slice_store<D>(v, lane, sys, sy, ey);
+  __syncthreads();
+  const int64_t tile = first / kTcN;
+  const int group = static_cast<int>((first % kTcN) / 8);
+  constexpr int kVecs = kRun / 8;  // 16-byte stores per run
+  for (int i = static_cast<int>(threadIdx.x); i < kChunks * kTcSlices * kVecs; i += 256) {
+    const int region = i / kVecs, part = i % kVecs;  // region = chunk * kTcSlices + slice
+    const int64_t block = tile * (kChunks * kTcSlices) + region;
+    uint4* dst = reinterpret_cast<uint4*>(sy + block * (kTcN * kTcKc) + group * kRun) + part;
+    *dst = reinterpret_cast<const uint4*>(staged + region * kRun)[part];
+  }
 }
 
 // Slices of A, one warp per row (computed once per solve).
